@@ -1,0 +1,380 @@
+#!/usr/bin/env python
+"""Throughput benchmark of the differentiable MLS-MPM stirring path on GB300.
+
+One step = one gradient evaluation of the identification loss: a recorded
+forward rollout (rod force profile) followed by the checkpointed adjoint,
+giving d loss / d viscosity parameters.  Default workload (one GPU): the 64^3
+single-scene configuration, 8 particles per cell (~604k particles), 2000
+substeps, checkpoint every 50, power-law fluid, rod moving on a circle.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  ``value`` is particle-substeps/s of forward +
+adjoint with inputs resident in HBM; ``e2e`` is the same metric through the
+public Python API with host (pinned) inputs copied in and results copied out
+every step.  ``--impl reference`` times the CPU restatement of the reference
+(oracle/, FP32, all host threads) on a bounded sample of the same workload.
+"""
+
+import argparse
+import glob
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = 'grad evals/s & particle-substeps/s, batched adjoint vs plain on GB300 @ grad err≤1e-3'
+UNIT = 'particle-substeps/s'
+
+# Algorithmic bytes of each kernel: (bytes per liquid particle, bytes per grid node)
+# p2g: read x,v,C,F (96) write F (36); grid result 16/node
+# grid: read P,M (16) write v (12) clear P,M (16)
+# g2p: read x (12) write x,v,C (60); read v grid 12/node
+# g2p_adj: read x (12), adj x,v,C (60), write adj x (12); read v 12, write grid adjoint 12 per node
+# grid_adj: read P,M 16, grid adjoint 12, write P/M adjoint 16, clear 12
+# p2g_adj: read state 96, adj F 36, adj x 12, write adj state 96; read P/M adjoint 16 per node
+KERNEL_BYTES = {
+    'p2g': (132, 16), 'grid': (0, 44), 'g2p': (72, 12),
+    'g2p_adj': (84, 24), 'grid_adj': (0, 56), 'p2g_adj': (240, 16),
+}
+KERNELS = ['p2g', 'grid', 'g2p', 'g2p_adj', 'grid_adj', 'p2g_adj', 'other']
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=5)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--config', default='C2')
+    ap.add_argument('--substeps', type=int, default=None, help='override the substep count')
+    ap.add_argument('--ckpt', type=int, default=None)
+    ap.add_argument('--p2g', type=int, default=None)
+    ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
+    ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
+    ap.add_argument('--no-e2e', action='store_true')
+    ap.add_argument('--no-cpu', action='store_true')
+    return ap.parse_args()
+
+
+# ---------------------------------------------------------------------------
+def dist_setup(args):
+    world = int(os.environ.get('WORLD_SIZE', '1'))
+    rank = int(os.environ.get('RANK', '0'))
+    local = int(os.environ.get('LOCAL_RANK', '0'))
+    return world, rank, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+    Q = ('index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,'
+         'clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,'
+         'clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, index):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix='.csv')
+            os.close(fd)
+            self.proc = subprocess.Popen(['nvidia-smi', '-i', str(self.index), '--query-gpu=' + self.Q,
+                                          '--format=csv,noheader,nounits', '-lms', '200'],
+                                         stdout=open(self.path, 'w'), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+
+    def stop(self):
+        if self.proc is None:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(',')]
+            if len(parts) < 9:
+                continue
+            try:
+                rows.append(parts)
+            except Exception:
+                pass
+        os.unlink(self.path)
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].replace('.', '', 1).isdigit()]
+        mx = [float(r[2]) for r in rows if r[2].replace('.', '', 1).isdigit()]
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        reasons = sorted({names[i] for r in rows for i in range(4) if r[5 + i].lower() == 'active'})
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': max(mx) if mx else None,
+                'reasons': reasons, 'samples': len(rows)}
+
+
+def peaks():
+    try:
+        p = json.load(open(os.path.join(ROOT, 'MEASURED_PEAKS.json')))
+        return float(p['hbm_gbs']), 'measured'
+    except Exception:
+        return 6800.0, 'fallback'
+
+
+def ncu_traffic(kernel, workload):
+    """dram bytes per launch of `kernel` from the committed ncu summary, if any."""
+    for path in glob.glob(os.path.join(ROOT, 'profiles', '*.md')) + glob.glob(os.path.join(ROOT, 'profiles', '*.txt')):
+        txt = open(path).read()
+        m = re.search(r'traffic_bytes_per_launch\[%s@%s\]\s*[:=]\s*([0-9.eE+]+)' % (re.escape(kernel), re.escape(workload)),
+                      txt)
+        if m:
+            return float(m.group(1))
+    return None
+
+
+def build_workload(args, rank):
+    from diffstir_gb300 import scene as S
+    cfg = S.CONFIGS[args.config]
+    T = args.substeps or cfg['n_steps']
+    sc = S.synthetic_scene(args.config, seed=rank, n_steps=T)
+    ckpt = args.ckpt or cfg['ckpt']
+    return sc, T, ckpt
+
+
+def workload_name(args, sc, T, ckpt):
+    d = sc.desc
+    return ('%s: %d^3 grid, %d particles (8/cell), %d substeps, checkpoint every %d, power-law fluid, '
+            'moving cylinder rod; forward + checkpointed adjoint' % (args.config, d.n_grid, sc.n_particles, T, ckpt))
+
+
+# ---------------------------------------------------------------------------
+def cpu_sample(sc, T_sample, threads):
+    """Oracle FP32 forward + adjoint of the first T_sample substeps."""
+    import oracle
+    T = T_sample
+    w = np.zeros((T, 3))
+    w[:, 0] = w[:, 2] = 1.0 / T
+    t0 = time.perf_counter()
+    oracle.grad(sc.desc, sc.params, sc.trajectory[:T + 1], T, sc.x0(), w, precision='f32', threads=threads)
+    return time.perf_counter() - t0
+
+
+def run_reference(args):
+    world, rank, local = dist_setup(args)
+    if rank != 0:
+        return 0
+    import oracle
+    oracle.build()
+    sc, T, ckpt = build_workload(args, 0)
+    threads = os.cpu_count() or 1
+    Ts = min(args.ref_sample, T)
+    for _ in range(args.warmup):
+        cpu_sample(sc, Ts, threads)
+    times = [cpu_sample(sc, Ts, threads) for _ in range(args.steps)]
+    dt = sum(times) / len(times)
+    val = sc.n_particles * Ts / dt
+    line = {
+        'metric': METRIC, 'value': val, 'unit': UNIT, 'n_gpus': args.gpus, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': dt * 1e3, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+        'impl': 'reference',
+        'config': {'workload': workload_name(args, sc, T, ckpt), 'parallelism': 'host threads'},
+        'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+                         'sample': 'first %d of %d substeps, forward + adjoint, per step' % (Ts, T)},
+        'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
+        'note': 'the reference is a Taichi program (Taichi is not installable offline); its CPU path is '
+                'timed through the line-by-line C++ restatement oracle/oracle.cpp (FP32, OpenMP)',
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+def run_ours(args):
+    import torch
+    world, rank, local = dist_setup(args)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl', device_id=torch.device('cuda', local))
+    torch.cuda.set_device(local)
+    from diffstir_gb300.simulator import Simulator
+    from diffstir_gb300 import scene as S
+
+    sc, T, ckpt = build_workload(args, rank)
+    opts = {}
+    if args.p2g is not None:
+        opts['p2g'] = args.p2g
+    sim = Simulator(sc, max_steps=T, options=opts)
+    dev = torch.device('cuda', local)
+    N = sc.n_particles
+
+    # target force profile from ground-truth parameters
+    true_p = torch.tensor(S.draw_params(np.random.default_rng(1000 + rank))[None], dtype=torch.float32, device=dev)
+    sim.set_params(true_p)
+    sim.reset()
+    target = sim.forward(T).clone()
+    params = torch.tensor(sc.params[None], dtype=torch.float32, device=dev)
+
+    def grad_eval(p):
+        sim.set_params(p)
+        sim.reset()
+        f = sim.forward(T, ckpt_every=ckpt, record=True)
+        diff = (f - target)[..., 0::2]
+        loss = (diff * diff).mean()
+        dF = torch.zeros_like(f)
+        dF[..., 0::2] = 2.0 * diff / diff.numel()
+        dp = sim.backward(dF)
+        return loss, dp
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    for _ in range(args.warmup):
+        grad_eval(params)
+    torch.cuda.synchronize()
+    st = sim.status()
+
+    clocks = ClockSampler(local)
+    clocks.start()
+    sim.set_option('profile', 1)
+    sim.set_option('launches', 0)
+    stream = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        loss, dp = grad_eval(params)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    ms = e0.elapsed_time(e1) / args.steps
+    launches = sim.get_option('launches')
+    prof = {k: (sim.get_option('prof_ns:' + k) / 1e6, sim.get_option('prof_count:' + k)) for k in KERNELS}
+    sim.set_option('profile', 0)
+    clk = clocks.stop()
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+        n_all = torch.tensor([float(N)], device=dev)
+        dist.all_reduce(n_all)
+        n_total = float(n_all.item())
+    else:
+        n_total = float(N)
+    value = n_total * T / (ms / 1e3)
+
+    # e2e through the public API with pinned host inputs / host results
+    e2e = None
+    if not args.no_e2e:
+        x0_h = torch.from_numpy(sc.x0()).float().pin_memory()
+        p_h = params.cpu().pin_memory()
+        tgt_h = target.cpu().pin_memory()
+        h2d = x0_h.numel() * 4 + p_h.numel() * 4 + tgt_h.numel() * 4
+        d2h = 4 * 4 + 4
+
+        def e2e_step():
+            x0_d = x0_h.to(dev, non_blocking=True)
+            p_d = p_h.to(dev, non_blocking=True)
+            t_d = tgt_h.to(dev, non_blocking=True)
+            sim.set_params(p_d)
+            sim.set_state(x0_d)
+            f = sim.forward(T, ckpt_every=ckpt, record=True)
+            diff = (f - t_d)[..., 0::2]
+            loss = (diff * diff).mean()
+            dF = torch.zeros_like(f)
+            dF[..., 0::2] = 2.0 * diff / diff.numel()
+            dp = sim.backward(dF)
+            return float(loss.item()), dp.cpu()
+
+        e2e_step()
+        barrier()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            e2e_step()
+        torch.cuda.synchronize()
+        e2e_ms = (time.perf_counter() - t0) * 1e3 / args.steps
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([e2e_ms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            e2e_ms = float(t.item())
+        e2e = {'value': n_total * T / (e2e_ms / 1e3), 'unit': UNIT, 'h2d_bytes_per_step': int(h2d),
+               'd2h_bytes_per_step': int(d2h), 'ms_per_step': e2e_ms}
+
+    if rank != 0:
+        return 0
+
+    # roofline of the dominant kernel (by total time inside the timed region)
+    G = sc.desc.n_grid ** 3
+    dom = max((k for k in KERNEL_BYTES), key=lambda k: prof[k][0])
+    tot_ms, cnt = prof[dom]
+    avg_s = tot_ms / 1e3 / max(cnt, 1)
+    bp, bn = KERNEL_BYTES[dom]
+    alg = bp * sc.desc.n_liquid + bn * G
+    hbm, peak_kind = peaks()
+    achieved = alg / avg_s / 1e9
+    wl = workload_name(args, sc, T, ckpt)
+    roof = {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
+            'frac': achieved / hbm, 'peak_kind': peak_kind, 'alg_bytes_per_launch': alg,
+            'avg_launch_us': avg_s * 1e6, 'traffic': ncu_traffic(dom, args.config)}
+    # whole-step algorithmic bytes: forward 192 N + 56 G, adjoint 480 N + 112 G per substep
+    step_bytes = T * ((192 + 480) * N + (56 + 112) * G)
+    kernel_share = {k: round(prof[k][0] / max(sum(v[0] for v in prof.values()), 1e-9), 4) for k in KERNELS}
+
+    cpu = None
+    if not args.no_cpu:
+        threads = os.cpu_count() or 1
+        Ts = min(args.cpu_sample, T)
+        dt = cpu_sample(sc, Ts, threads)
+        cpu = {'value': N * Ts / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+               'sample': 'oracle FP32 forward + adjoint of the first %d of %d substeps of the same scene' % (Ts, T)}
+
+    line = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+        'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
+        'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
+        'config': {'workload': wl, 'grid': G, 'particles': N, 'substeps': T, 'ckpt_every': ckpt,
+                   'scenes_per_gpu': 1, 'parallelism': 'one scene per GPU (scene-sharded)',
+                   'l2': 'inputs larger than L2 (checkpoints + segment states ~%.1f GB per step)' %
+                         ((T // ckpt + ckpt) * N * 96 / 1e9)},
+        'grad_evals_per_s': world * 1e3 / ms,
+        'forward_adjoint_roofline_frac': step_bytes / (ms / 1e3) / 1e9 / hbm,
+        'roofline': roof,
+        'kernel_time_share': kernel_share,
+        'cpu_baseline': cpu,
+        'e2e': e2e,
+        'gpu_launches': int(launches),
+        'clocks': clk,
+        'status_flags': int(st),
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == 'reference':
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == '__main__':
+    sys.exit(main())

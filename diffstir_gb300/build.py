@@ -1,0 +1,74 @@
+"""In-tree build of the CUDA extension libdiffstir.so for sm_103a.
+
+The three translation units under csrc/ are compiled in parallel with nvcc
+(``-gencode arch=compute_103a,code=sm_103a``) and linked into
+``diffstir_gb300/_build/libdiffstir.so``, a plain shared library exporting the
+C ABI of include/diffstir.h.  No torch headers are involved.
+"""
+
+import concurrent.futures
+import os
+import shutil
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, 'csrc')
+OUT_DIR = os.path.join(HERE, '_build')
+LIB = os.path.join(OUT_DIR, 'libdiffstir.so')
+SOURCES = ['kernels.cu', 'svd.cu', 'api.cu']
+HEADERS = ['common.cuh', 'svd.cuh', 'internal.h']
+ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
+NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2',
+              '--expt-relaxed-constexpr']
+
+
+def nvcc_path():
+    for cand in (os.environ.get('NVCC'), shutil.which('nvcc'), '/usr/local/cuda/bin/nvcc'):
+        if cand and os.path.exists(cand):
+            return cand
+    raise RuntimeError('nvcc not found')
+
+
+def _inputs():
+    files = [os.path.join(CSRC, s) for s in SOURCES + HEADERS]
+    files.append(os.path.join(HERE, '..', 'include', 'diffstir.h'))
+    return files
+
+
+def up_to_date():
+    if not os.path.exists(LIB):
+        return False
+    t = os.path.getmtime(LIB)
+    return all(os.path.getmtime(f) <= t for f in _inputs())
+
+
+def build(force=False, verbose=False, extra_flags=()):
+    if not force and up_to_date():
+        return LIB
+    os.makedirs(OUT_DIR, exist_ok=True)
+    nvcc = nvcc_path()
+    inc = ['-I', os.path.join(HERE, '..', 'include')]
+
+    def compile_one(src):
+        obj = os.path.join(OUT_DIR, os.path.splitext(src)[0] + '.o')
+        cmd = [nvcc] + ARCH + NVCC_FLAGS + list(extra_flags) + inc + ['-c', os.path.join(CSRC, src), '-o', obj]
+        r = subprocess.run(cmd, capture_output=True, text=True)
+        if r.returncode != 0:
+            raise RuntimeError('nvcc failed for %s:\n%s\n%s' % (src, ' '.join(cmd), r.stderr))
+        if verbose and r.stderr:
+            print(r.stderr)
+        return obj
+
+    with concurrent.futures.ThreadPoolExecutor(len(SOURCES)) as ex:
+        objs = list(ex.map(compile_one, SOURCES))
+    tmp = LIB + '.tmp%d' % os.getpid()
+    cmd = [nvcc] + ARCH + ['-shared', '-o', tmp] + objs
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError('nvcc link failed:\n%s\n%s' % (' '.join(cmd), r.stderr))
+    os.replace(tmp, LIB)
+    return LIB
+
+
+if __name__ == '__main__':
+    print(build(force=True, verbose=True))

@@ -1,0 +1,659 @@
+// C ABI (include/diffstir.h): handle, device memory, substep orchestration,
+// checkpointed forward rollout and the segment-recomputing reverse pass.
+//
+// The reference keeps the whole trajectory ([max_steps, N] fields,
+// src/simulator/initialization.py:155-158) so that ti.ad.Tape can replay
+// backward(s) (simulation_functions.py:351-365) from stored states.  Here the
+// forward keeps only a checkpoint every K substeps; the reverse pass walks the
+// segments last to first, recomputes one segment (keeping its K states and K
+// P2G grids), then runs the adjoint substeps of that segment in reverse.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+using namespace dstir;
+
+namespace {
+// kernel kinds timed by the optional in-library profiler
+enum { K_P2G = 0, K_GRID, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_OTHER, K_NUM };
+const char* const kKernelNames[K_NUM] = {"p2g", "grid", "g2p", "g2p_adj", "grid_adj", "p2g_adj", "other"};
+
+// CUDA-event timing of every launch on the launching stream.  Event pairs live
+// in a ring; a pair is read back (synchronising on its stop event) when the
+// ring wraps or when the totals are queried.
+struct Profiler {
+    bool on = false;
+    std::vector<cudaEvent_t> start, stop;
+    std::vector<int> kind;
+    size_t head = 0, pending = 0;
+    double total_ms[K_NUM] = {0};
+    long long count[K_NUM] = {0};
+
+    void reset() {
+        drain();
+        for (int k = 0; k < K_NUM; ++k) {
+            total_ms[k] = 0;
+            count[k] = 0;
+        }
+    }
+    void ensure() {
+        if (!start.empty()) return;
+        const size_t n = 4096;
+        start.resize(n);
+        stop.resize(n);
+        kind.resize(n);
+        for (size_t i = 0; i < n; ++i) {
+            cudaEventCreate(&start[i]);
+            cudaEventCreate(&stop[i]);
+        }
+    }
+    void consume(size_t i) {
+        cudaEventSynchronize(stop[i]);
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, start[i], stop[i]) == cudaSuccess) {
+            total_ms[kind[i]] += ms;
+            count[kind[i]] += 1;
+        }
+    }
+    void drain() {
+        size_t n = start.size();
+        while (pending > 0) {
+            size_t i = (head + n - pending) % n;
+            consume(i);
+            --pending;
+        }
+    }
+    size_t begin(int k, cudaStream_t st) {
+        ensure();
+        size_t n = start.size();
+        if (pending == n) {
+            consume((head + n - pending) % n);
+            --pending;
+        }
+        size_t i = head;
+        kind[i] = k;
+        cudaEventRecord(start[i], st);
+        return i;
+    }
+    void end(size_t i, cudaStream_t st) {
+        cudaEventRecord(stop[i], st);
+        head = (head + 1) % start.size();
+        ++pending;
+    }
+    void destroy() {
+        for (auto e : start) cudaEventDestroy(e);
+        for (auto e : stop) cudaEventDestroy(e);
+        start.clear();
+        stop.clear();
+    }
+};
+}  // namespace
+
+struct DstirHandle {
+    int B = 0;
+    int max_steps = 0;
+    std::vector<DstirSceneDesc> desc;
+    std::vector<SceneDev> sc_h;
+    long long N = 0, stride = 0, G = 0;
+    int block = 256, gblock = 256, p2g_variant = P2G_VEC, use_graph = 0;
+    std::vector<BlockInfo> blk_h;
+    std::vector<GridBlock> gblk_h;
+    SceneDev* sc = nullptr;
+    BlockInfo* blk = nullptr;
+    GridBlock* gblk = nullptr;
+    int n_blocks = 0, n_gblocks = 0;
+
+    float* work = nullptr;   // 2 state slots
+    float* ckpt = nullptr;
+    long long ckpt_slots = 0;
+    float* seg = nullptr;
+    long long seg_slots = 0;
+    float4* pm = nullptr;     // grid slots (P2G result)
+    float4* vo = nullptr;     // grid slots (velocity out)
+    long long grid_slots = 0;
+    float4* ga = nullptr;
+    float4* pmb = nullptr;
+    float* adj = nullptr;     // 2 adjoint slots
+    float* traj = nullptr;
+    float* params = nullptr;
+    int* models = nullptr;
+    float* force_scratch = nullptr;  // [B][max_steps][3]
+    float* pgrad = nullptr;          // [max_steps][B][4]
+    float* partial = nullptr;
+    long long partial_len = 0;
+    unsigned* counters = nullptr;
+    unsigned* status = nullptr;
+
+    Profiler prof;
+    long long launches = 0;  // kernel launches issued since the counter was reset
+
+    int cur = 0;  // work slot holding the current state
+    bool recorded = false;
+    int rec_t0 = 0, rec_n = 0, rec_K = 0;
+    std::string err;
+};
+
+namespace {
+
+int fail(DstirHandle* h, int code, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (h) h->err = buf;
+    return code;
+}
+
+#define CUDA_TRY(h, expr)                                                                      \
+    do {                                                                                       \
+        cudaError_t e_ = (expr);                                                               \
+        if (e_ != cudaSuccess)                                                                 \
+            return fail((h), DSTIR_ECUDA, "%s failed: %s", #expr, cudaGetErrorString(e_));    \
+    } while (0)
+
+template <class T>
+int dalloc(DstirHandle* h, T** p, size_t count, const char* what) {
+    if (*p) cudaFree(*p);
+    *p = nullptr;
+    if (count == 0) count = 1;
+    cudaError_t e = cudaMalloc((void**)p, count * sizeof(T));
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        cudaGetLastError();
+        return fail(h, DSTIR_ENOMEM, "cudaMalloc of %zu bytes for %s failed: %s", count * sizeof(T), what,
+                    cudaGetErrorString(e));
+    }
+    return DSTIR_OK;
+}
+
+inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+size_t slot_floats(const DstirHandle* h) { return (size_t)NS * (size_t)h->stride; }
+
+int build_tables(DstirHandle* h) {
+    h->blk_h.clear();
+    h->gblk_h.clear();
+    for (int s = 0; s < h->B; ++s) {
+        const SceneDev& sd = h->sc_h[s];
+        long long starts[3] = {sd.p0, sd.p0 + sd.n_liquid, sd.p0 + sd.n_liquid + sd.n_rod};
+        long long counts[3] = {sd.n_liquid, sd.n_rod, sd.n_container};
+        for (int kd = 0; kd < 3; ++kd) {
+            long long nb = (counts[kd] + h->block - 1) / h->block;
+            for (long long b = 0; b < nb; ++b) {
+                BlockInfo bi;
+                bi.scene = s;
+                bi.kind = kd;
+                bi.idx = (int)b;
+                bi.count = (int)nb;
+                bi.start = starts[kd] + b * h->block;
+                bi.end = std::min(starts[kd] + counts[kd], bi.start + h->block);
+                h->blk_h.push_back(bi);
+            }
+        }
+        long long gn = (long long)sd.n * sd.n * sd.n;
+        long long nb = (gn + h->gblock - 1) / h->gblock;
+        for (long long b = 0; b < nb; ++b) {
+            GridBlock gb;
+            gb.scene = s;
+            gb.idx = (int)b;
+            gb.count = (int)nb;
+            gb.pad = 0;
+            gb.start = sd.goff + b * h->gblock;
+            gb.end = std::min(sd.goff + gn, gb.start + h->gblock);
+            h->gblk_h.push_back(gb);
+        }
+    }
+    h->n_blocks = (int)h->blk_h.size();
+    h->n_gblocks = (int)h->gblk_h.size();
+    int rc;
+    if ((rc = dalloc(h, &h->blk, h->blk_h.size(), "block table"))) return rc;
+    if ((rc = dalloc(h, &h->gblk, h->gblk_h.size(), "grid block table"))) return rc;
+    CUDA_TRY(h, cudaMemcpy(h->blk, h->blk_h.data(), h->blk_h.size() * sizeof(BlockInfo), cudaMemcpyHostToDevice));
+    CUDA_TRY(h, cudaMemcpy(h->gblk, h->gblk_h.data(), h->gblk_h.size() * sizeof(GridBlock),
+                           cudaMemcpyHostToDevice));
+    long long pl = std::max<long long>(std::max(h->n_blocks, h->n_gblocks), 1);
+    if (pl > h->partial_len) {
+        if ((rc = dalloc(h, &h->partial, (size_t)pl * 4, "partial sums"))) return rc;
+        h->partial_len = pl;
+    }
+    return DSTIR_OK;
+}
+
+int ensure_grid_slots(DstirHandle* h, long long n) {
+    if (n <= h->grid_slots) return DSTIR_OK;
+    int rc;
+    if ((rc = dalloc(h, &h->pm, (size_t)(n * h->G), "P2G grids"))) return rc;
+    if ((rc = dalloc(h, &h->vo, (size_t)(n * h->G), "velocity grids"))) return rc;
+    h->grid_slots = n;
+    CUDA_TRY(h, cudaMemset(h->pm, 0, (size_t)(n * h->G) * sizeof(float4)));
+    return DSTIR_OK;
+}
+
+FwdArgs fwd_args(DstirHandle* h, const float* cur, float* next, float4* pm, float4* vo, int f, float* force,
+                 long long force_stride, int fo, int clear_pm) {
+    FwdArgs a;
+    a.sc = h->sc;
+    a.blk = h->blk;
+    a.gblk = h->gblk;
+    a.cur = cur;
+    a.next = next;
+    a.stride = h->stride;
+    a.pm = pm;
+    a.vo = vo;
+    a.traj = h->traj;
+    a.traj_len = h->max_steps + 1;
+    a.f = f;
+    a.params = h->params;
+    a.models = h->models;
+    a.force = force;
+    a.force_stride = force_stride;
+    a.fo = fo;
+    a.partial = h->partial;
+    a.counters = h->counters;
+    a.status = h->status;
+    a.clear_pm = clear_pm;
+    a.batch = h->B;
+    return a;
+}
+
+// Issue one kernel launch, bracketed by profiler events when profiling is on.
+template <class Fn>
+void timed(DstirHandle* h, int kind, cudaStream_t st, Fn fn) {
+    ++h->launches;
+    if (!h->prof.on) {
+        fn();
+        return;
+    }
+    size_t i = h->prof.begin(kind, st);
+    fn();
+    h->prof.end(i, st);
+}
+
+void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st) {
+    timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, st); });
+    timed(h, K_GRID, st, [&] { launch_grid(a, h->n_gblocks, h->gblock, st); });
+    timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st); });
+}
+
+void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st) {
+    int var = h->p2g_variant == P2G_PLAIN ? P2G_PLAIN : P2G_VEC;
+    timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st); });
+    timed(h, K_GRID_ADJ, st, [&] { launch_grid_adj(a, h->n_gblocks, h->gblock, st); });
+    timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, st); });
+}
+
+}  // namespace
+
+extern "C" {
+
+int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps, DstirHandle** out) {
+    if (!out) return DSTIR_EINVAL;
+    *out = nullptr;
+    if (!scenes || batch <= 0 || max_steps <= 0) return DSTIR_EINVAL;
+    DstirHandle* h = new (std::nothrow) DstirHandle();
+    if (!h) return DSTIR_ENOMEM;
+    h->B = batch;
+    h->max_steps = max_steps;
+    h->desc.assign(scenes, scenes + batch);
+    long long p0 = 0, g0 = 0;
+    for (int s = 0; s < batch; ++s) {
+        const DstirSceneDesc& d = scenes[s];
+        if (d.n_grid < 4 || d.n_grid > 1024 || d.n_liquid < 0 || d.n_rod < 0 || d.n_container < 0 ||
+            d.bound < 0 || !(d.dt > 0.f) || d.model < 0 || d.model > 2 || d.rod_mode < 0 || d.rod_mode > 1 ||
+            d.j_mode < 0 || d.j_mode > 1) {
+            int rc = fail(h, DSTIR_EINVAL, "scene %d: invalid descriptor", s);
+            delete h;
+            return rc;
+        }
+        if (d.rod_mode == DSTIR_ROD_CYLINDER && d.n_rod != 0) {
+            delete h;
+            return DSTIR_EINVAL;
+        }
+        SceneDev sd;
+        memset(&sd, 0, sizeof(sd));
+        sd.n = d.n_grid;
+        sd.bound = d.bound;
+        sd.rod_mode = d.rod_mode;
+        sd.j_mode = d.j_mode;
+        sd.container_wall = d.container_wall;
+        sd.model = d.model;
+        sd.n_liquid = d.n_liquid;
+        sd.n_rod = d.n_rod;
+        sd.n_container = d.n_container;
+        sd.p0 = p0;
+        sd.goff = g0;
+        sd.dt = d.dt;
+        sd.dx = 1.f / (float)d.n_grid;
+        sd.inv_dx = (float)d.n_grid;
+        sd.gravity = d.gravity;
+        sd.bulk = d.bulk_modulus;
+        sd.alpha = (-d.dt * d.liquid_p_vol * 4.f * sd.inv_dx * sd.inv_dx);
+        sd.m_liq = d.liquid_p_mass;
+        sd.m_rod = d.rod_p_mass;
+        sd.m_cont = d.container_p_mass;
+        sd.force_scale = d.force_scale;
+        sd.ccx = d.container_cx;
+        sd.ccz = d.container_cz;
+        sd.cr2 = d.container_r * d.container_r;
+        sd.rod_r2 = d.rod_radius * d.rod_radius;
+        h->sc_h.push_back(sd);
+        p0 += (long long)d.n_liquid + d.n_rod + d.n_container;
+        g0 += (long long)d.n_grid * d.n_grid * d.n_grid;
+    }
+    h->N = p0;
+    h->stride = std::max<long long>((p0 + 31) / 32 * 32, 32);
+    h->G = g0;
+    int rc = DSTIR_OK;
+    std::vector<int> models(batch);
+    for (int s = 0; s < batch; ++s) models[s] = scenes[s].model;
+    if ((rc = dalloc(h, &h->sc, batch, "scene table")) ||
+        (rc = dalloc(h, &h->work, 2 * slot_floats(h), "state")) ||
+        (rc = dalloc(h, &h->adj, 2 * slot_floats(h), "adjoint state")) ||
+        (rc = dalloc(h, &h->ga, (size_t)h->G, "grid adjoint")) ||
+        (rc = dalloc(h, &h->pmb, (size_t)h->G, "P2G adjoint")) ||
+        (rc = dalloc(h, &h->traj, (size_t)batch * (max_steps + 1) * 3, "trajectory")) ||
+        (rc = dalloc(h, &h->params, (size_t)batch * 4, "parameters")) ||
+        (rc = dalloc(h, &h->models, (size_t)batch, "models")) ||
+        (rc = dalloc(h, &h->force_scratch, (size_t)batch * max_steps * 3, "force scratch")) ||
+        (rc = dalloc(h, &h->pgrad, (size_t)max_steps * batch * 4, "parameter gradients")) ||
+        (rc = dalloc(h, &h->counters, (size_t)3 * batch, "counters")) ||
+        (rc = dalloc(h, &h->status, 1, "status")) || (rc = ensure_grid_slots(h, 1)) || (rc = build_tables(h))) {
+        std::string msg = h->err;
+        dstir_destroy(h);
+        return rc;
+    }
+    cudaError_t e = cudaMemcpy(h->sc, h->sc_h.data(), batch * sizeof(SceneDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(h->models, models.data(), batch * sizeof(int), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemset(h->counters, 0, 3 * batch * sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(h->status, 0, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemset(h->ga, 0, (size_t)h->G * sizeof(float4));
+    if (e == cudaSuccess) e = cudaMemset(h->params, 0, (size_t)batch * 4 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(h->traj, 0, (size_t)batch * (max_steps + 1) * 3 * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(h->work, 0, 2 * slot_floats(h) * sizeof(float));
+    if (e != cudaSuccess) {
+        dstir_destroy(h);
+        return DSTIR_ECUDA;
+    }
+    *out = h;
+    return DSTIR_OK;
+}
+
+void dstir_destroy(DstirHandle* h) {
+    if (!h) return;
+    h->prof.drain();
+    h->prof.destroy();
+    void* ptrs[] = {h->sc, h->blk, h->gblk, h->work, h->ckpt, h->seg, h->pm, h->vo, h->ga, h->pmb, h->adj,
+                    h->traj, h->params, h->models, h->force_scratch, h->pgrad, h->partial, h->counters, h->status};
+    for (void* p : ptrs)
+        if (p) cudaFree(p);
+    delete h;
+}
+
+const char* dstir_last_error(const DstirHandle* h) { return h ? h->err.c_str() : "null handle"; }
+
+int dstir_num_particles(const DstirHandle* h, int64_t* n_total, int32_t* batch) {
+    if (!h) return DSTIR_EINVAL;
+    if (n_total) *n_total = h->N;
+    if (batch) *batch = h->B;
+    return DSTIR_OK;
+}
+
+int dstir_set_state(DstirHandle* h, const float* x, const float* v, const float* C, const float* F, void* stream) {
+    if (!h) return DSTIR_EINVAL;
+    if (!x) return fail(h, DSTIR_EINVAL, "dstir_set_state: x is required");
+    h->cur = 0;
+    h->recorded = false;
+    timed(h, K_OTHER, S(stream), [&] { launch_pack_state(x, v, C, F, h->work, h->stride, h->N, S(stream)); });
+    CUDA_TRY(h, cudaGetLastError());
+    return DSTIR_OK;
+}
+
+int dstir_get_state(DstirHandle* h, float* x, float* v, float* C, float* F, void* stream) {
+    if (!h) return DSTIR_EINVAL;
+    launch_unpack_state(h->work + (size_t)h->cur * slot_floats(h), h->stride, h->N, x, v, C, F, S(stream));
+    CUDA_TRY(h, cudaGetLastError());
+    return DSTIR_OK;
+}
+
+int dstir_set_params(DstirHandle* h, const float* params, const int32_t* models, void* stream) {
+    if (!h) return DSTIR_EINVAL;
+    if (params)
+        CUDA_TRY(h, cudaMemcpyAsync(h->params, params, (size_t)h->B * 4 * sizeof(float), cudaMemcpyDeviceToDevice,
+                                    S(stream)));
+    if (models)
+        CUDA_TRY(h, cudaMemcpyAsync(h->models, models, (size_t)h->B * sizeof(int), cudaMemcpyDeviceToDevice,
+                                    S(stream)));
+    h->recorded = false;
+    return DSTIR_OK;
+}
+
+int dstir_set_trajectory(DstirHandle* h, const float* traj, void* stream) {
+    if (!h || !traj) return DSTIR_EINVAL;
+    CUDA_TRY(h, cudaMemcpyAsync(h->traj, traj, (size_t)h->B * (h->max_steps + 1) * 3 * sizeof(float),
+                                cudaMemcpyDeviceToDevice, S(stream)));
+    h->recorded = false;
+    return DSTIR_OK;
+}
+
+int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every, int32_t record, float* force_out,
+                  void* stream) {
+    if (!h) return DSTIR_EINVAL;
+    if (t0 < 0 || nsteps < 0 || (long long)t0 + nsteps > h->max_steps)
+        return fail(h, DSTIR_EINVAL, "dstir_forward: steps [%d, %d) outside [0, %d)", t0, t0 + nsteps, h->max_steps);
+    if (record && ckpt_every <= 0) return fail(h, DSTIR_EINVAL, "dstir_forward: ckpt_every must be > 0");
+    cudaStream_t st = S(stream);
+    h->recorded = false;
+    if (nsteps == 0) return DSTIR_OK;
+    int K = record ? std::min(ckpt_every, nsteps) : 1;
+    long long nseg = record ? (nsteps + K - 1) / K : 0;
+    int rc;
+    if (record && nseg > h->ckpt_slots) {
+        if ((rc = dalloc(h, &h->ckpt, (size_t)nseg * slot_floats(h), "checkpoints"))) return rc;
+        h->ckpt_slots = nseg;
+    }
+    float* force = force_out ? force_out : h->force_scratch;
+    long long fstride = force_out ? (long long)nsteps * 3 : (long long)h->max_steps * 3;
+    size_t sf = slot_floats(h);
+    float* W[2] = {h->work, h->work + sf};
+    float* curp = W[h->cur];
+    if (record) CUDA_TRY(h, cudaMemcpyAsync(h->ckpt, curp, sf * sizeof(float), cudaMemcpyDeviceToDevice, st));
+    CUDA_TRY(h, cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st));
+    for (int k = 0; k < nsteps; ++k) {
+        bool boundary = record && ((k + 1) % K == 0) && (k + 1 < nsteps);
+        float* dst = boundary ? h->ckpt + (size_t)((k + 1) / K) * sf : (curp == W[0] ? W[1] : W[0]);
+        FwdArgs a = fwd_args(h, curp, dst, h->pm, h->vo, t0 + k, force, fstride, k, 1);
+        run_substep(h, a, st);
+        curp = dst;
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    h->cur = (curp == W[0]) ? 0 : 1;
+    if (record) {
+        h->recorded = true;
+        h->rec_t0 = t0;
+        h->rec_n = nsteps;
+        h->rec_K = K;
+    }
+    return DSTIR_OK;
+}
+
+int dstir_substep(DstirHandle* h, int32_t f, float* force_out, void* stream) {
+    if (!h) return DSTIR_EINVAL;
+    if (f < 0 || f >= h->max_steps) return fail(h, DSTIR_EINVAL, "dstir_substep: f=%d outside [0,%d)", f, h->max_steps);
+    cudaStream_t st = S(stream);
+    h->recorded = false;
+    size_t sf = slot_floats(h);
+    float* W[2] = {h->work, h->work + sf};
+    float* force = force_out ? force_out : h->force_scratch;
+    long long fstride = force_out ? 3 : (long long)h->max_steps * 3;
+    int fo = force_out ? 0 : f;
+    FwdArgs a = fwd_args(h, W[h->cur], W[1 - h->cur], h->pm, h->vo, f, force, fstride, fo, 1);
+    run_substep(h, a, st);
+    CUDA_TRY(h, cudaGetLastError());
+    h->cur = 1 - h->cur;
+    return DSTIR_OK;
+}
+
+int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, float* dL_dx0, float* dL_dv0,
+                   float* dL_dC0, float* dL_dF0, void* stream) {
+    if (!h) return DSTIR_EINVAL;
+    if (!h->recorded) return fail(h, DSTIR_ESTATE, "dstir_backward: no recorded forward (record=1) to differentiate");
+    if (!dL_dforce) return fail(h, DSTIR_EINVAL, "dstir_backward: dL_dforce is required");
+    cudaStream_t st = S(stream);
+    const int n = h->rec_n, K = h->rec_K, t0 = h->rec_t0;
+    const long long nseg = (n + K - 1) / K;
+    size_t sf = slot_floats(h);
+    int rc;
+    if (K > h->seg_slots) {
+        if ((rc = dalloc(h, &h->seg, (size_t)K * sf, "segment states"))) return rc;
+        h->seg_slots = K;
+    }
+    if ((rc = ensure_grid_slots(h, K))) return rc;
+    float* A[2] = {h->adj, h->adj + sf};
+    int nx = 0;
+    CUDA_TRY(h, cudaMemsetAsync(A[nx], 0, sf * sizeof(float), st));
+    CUDA_TRY(h, cudaMemsetAsync(h->ga, 0, (size_t)h->G * sizeof(float4), st));
+    CUDA_TRY(h, cudaMemsetAsync(h->pgrad, 0, (size_t)n * h->B * 4 * sizeof(float), st));
+    const long long fstride = (long long)n * 3;
+    for (long long sgi = nseg - 1; sgi >= 0; --sgi) {
+        int s0 = (int)(sgi * K);
+        int L = std::min(K, n - s0);
+        float* slot0 = h->ckpt + (size_t)sgi * sf;
+        auto slot = [&](int j) -> float* { return j == 0 ? slot0 : h->seg + (size_t)(j - 1) * sf; };
+        CUDA_TRY(h, cudaMemsetAsync(h->pm, 0, (size_t)L * h->G * sizeof(float4), st));
+        for (int k = 0; k < L; ++k) {
+            FwdArgs a = fwd_args(h, slot(k), slot(k + 1), h->pm + (size_t)k * h->G, h->vo + (size_t)k * h->G,
+                                 t0 + s0 + k, h->force_scratch, (long long)h->max_steps * 3, t0 + s0 + k, 0);
+            run_substep(h, a, st);
+        }
+        for (int k = L - 1; k >= 0; --k) {
+            AdjArgs a;
+            a.sc = h->sc;
+            a.blk = h->blk;
+            a.gblk = h->gblk;
+            a.cur = slot(k);
+            a.stride = h->stride;
+            a.pm = h->pm + (size_t)k * h->G;
+            a.vo = h->vo + (size_t)k * h->G;
+            a.ga = h->ga;
+            a.pmb = h->pmb;
+            a.adj_next = A[nx];
+            a.adj_cur = A[1 - nx];
+            a.traj = h->traj;
+            a.traj_len = h->max_steps + 1;
+            a.f = t0 + s0 + k;
+            a.params = h->params;
+            a.models = h->models;
+            a.dforce = dL_dforce;
+            a.dforce_stride = fstride;
+            a.fo = s0 + k;
+            a.pgrad = h->pgrad;
+            a.partial = h->partial;
+            a.counters = h->counters;
+            a.batch = h->B;
+            run_adj_substep(h, a, st);
+            nx = 1 - nx;
+        }
+    }
+    CUDA_TRY(h, cudaGetLastError());
+    CUDA_TRY(h, cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st));
+    if (dL_dparams) timed(h, K_OTHER, st, [&] { launch_reduce_pgrad(h->pgrad, n, h->B, dL_dparams, st); });
+    if (dL_dx0 || dL_dv0 || dL_dC0 || dL_dF0)
+        timed(h, K_OTHER, st,
+              [&] { launch_unpack_state(A[nx], h->stride, h->N, dL_dx0, dL_dv0, dL_dC0, dL_dF0, st); });
+    CUDA_TRY(h, cudaGetLastError());
+    return DSTIR_OK;
+}
+
+int dstir_status(DstirHandle* h, uint32_t* flags, void* stream) {
+    if (!h || !flags) return DSTIR_EINVAL;
+    unsigned v = 0;
+    CUDA_TRY(h, cudaMemcpyAsync(&v, h->status, sizeof(unsigned), cudaMemcpyDeviceToHost, S(stream)));
+    CUDA_TRY(h, cudaStreamSynchronize(S(stream)));
+    CUDA_TRY(h, cudaMemsetAsync(h->status, 0, sizeof(unsigned), S(stream)));
+    *flags = v;
+    return DSTIR_OK;
+}
+
+int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
+    if (!h || !key) return DSTIR_EINVAL;
+    if (!strcmp(key, "p2g")) {
+        if (value < 0 || value > 2) return fail(h, DSTIR_EINVAL, "p2g variant %lld not in 0..2", (long long)value);
+        h->p2g_variant = (int)value;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "block") || !strcmp(key, "gblock")) {
+        if (value != 64 && value != 128 && value != 256)
+            return fail(h, DSTIR_EINVAL, "%s must be 64, 128 or 256", key);
+        if (!strcmp(key, "block"))
+            h->block = (int)value;
+        else
+            h->gblock = (int)value;
+        h->recorded = false;
+        return build_tables(h);
+    }
+    if (!strcmp(key, "graph")) {
+        h->use_graph = value ? 1 : 0;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "profile")) {  // 1: time every launch with CUDA events; resets the totals
+        h->prof.reset();
+        h->prof.on = value != 0;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "launches")) {  // reset the launch counter
+        h->launches = value;
+        return DSTIR_OK;
+    }
+    return fail(h, DSTIR_EINVAL, "unknown option '%s'", key);
+}
+
+int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
+    if (!h || !key || !value) return DSTIR_EINVAL;
+    if (!strcmp(key, "p2g")) *value = h->p2g_variant;
+    else if (!strcmp(key, "block")) *value = h->block;
+    else if (!strcmp(key, "gblock")) *value = h->gblock;
+    else if (!strcmp(key, "graph")) *value = h->use_graph;
+    else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
+    else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
+    else if (!strcmp(key, "stride")) *value = h->stride;
+    else if (!strcmp(key, "launches")) *value = h->launches;
+    else if (!strncmp(key, "prof_ns:", 8) || !strncmp(key, "prof_count:", 11)) {
+        // totals of the in-library profiler for one kernel kind ("prof_ns:p2g", "prof_count:p2g")
+        bool ns = key[5] == 'n';
+        const char* name = key + (ns ? 8 : 11);
+        DstirHandle* hm = const_cast<DstirHandle*>(h);
+        hm->prof.drain();
+        for (int k = 0; k < K_NUM; ++k)
+            if (!strcmp(name, kKernelNames[k])) {
+                *value = ns ? (int64_t)(hm->prof.total_ms[k] * 1e6) : (int64_t)hm->prof.count[k];
+                return DSTIR_OK;
+            }
+        return DSTIR_EINVAL;
+    } else return DSTIR_EINVAL;
+    return DSTIR_OK;
+}
+
+int dstir_svd3(const float* A, float* U, float* Sg, float* V, int64_t n, void* stream) {
+    if (n < 0 || (n > 0 && (!A || !U || !Sg || !V))) return DSTIR_EINVAL;
+    launch_svd3(A, U, Sg, V, n, S(stream));
+    return cudaGetLastError() == cudaSuccess ? DSTIR_OK : DSTIR_ECUDA;
+}
+
+int dstir_svd3_backward(const float* gU, const float* gS, const float* gV, const float* U, const float* Sg,
+                        const float* V, float* gA, int64_t n, void* stream) {
+    if (n < 0 || (n > 0 && (!gU || !gS || !gV || !U || !Sg || !V || !gA))) return DSTIR_EINVAL;
+    launch_svd3_backward(gU, gS, gV, U, Sg, V, gA, n, S(stream));
+    return cudaGetLastError() == cudaSuccess ? DSTIR_OK : DSTIR_ECUDA;
+}
+
+}  // extern "C"

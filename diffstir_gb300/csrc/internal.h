@@ -1,0 +1,82 @@
+// Host-side launch interface between the orchestration (api.cu) and the
+// kernels (kernels.cu, svd.cu).  Not part of the public C ABI.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+
+namespace dstir {
+
+struct FwdArgs {
+    const SceneDev* sc;
+    const BlockInfo* blk;
+    const GridBlock* gblk;
+    const float* cur;       // state at substep f (SoA, `stride` per component)
+    float* next;            // state at substep f+1
+    long long stride;
+    float4* pm;             // grid momentum (xyz) + mass (w) of this substep
+    float4* vo;             // grid velocity after the boundary conditions
+    const float* traj;      // [B][traj_len][3]
+    int traj_len;
+    int f;                  // substep index (trajectory entries f, f+1)
+    const float* params;    // [B][4]
+    const int* models;      // [B]
+    float* force;           // force[s*force_stride + fo*3 + c]
+    long long force_stride;
+    int fo;
+    float* partial;         // [n_blocks][4] per-block partial sums
+    unsigned* counters;     // per-scene arrival counters
+    unsigned* status;       // DSTIR_STATUS_* word
+    int clear_pm;           // grid kernel zeroes pm after reading it
+    int batch;
+};
+
+struct AdjArgs {
+    const SceneDev* sc;
+    const BlockInfo* blk;
+    const GridBlock* gblk;
+    const float* cur;        // state at substep f
+    long long stride;
+    const float4* pm;        // P2G result of substep f
+    const float4* vo;        // grid velocity of substep f
+    float4* ga;              // adjoint of vo (scatter target, zeroed by the grid adjoint)
+    float4* pmb;             // adjoint of pm
+    const float* adj_next;   // adjoint of the state at f+1
+    float* adj_cur;          // adjoint of the state at f
+    const float* traj;
+    int traj_len;
+    int f;
+    const float* params;
+    const int* models;
+    const float* dforce;     // dL/dforce, same layout as FwdArgs::force
+    long long dforce_stride;
+    int fo;
+    float* pgrad;            // [T][B][4] per-substep parameter gradients
+    float* partial;
+    unsigned* counters;
+    int batch;
+};
+
+// p2g variants
+enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_TILE = 2 };
+
+void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, cudaStream_t st);
+void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st);
+void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st);
+
+void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st);
+void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st);
+void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, cudaStream_t st);
+
+void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
+                       long long stride, long long n, cudaStream_t s);
+void launch_unpack_state(const float* st, long long stride, long long n, float* x, float* v, float* C,
+                         float* F, cudaStream_t s);
+void launch_reduce_pgrad(const float* pgrad, int T, int B, float* out, cudaStream_t s);
+
+void launch_svd3(const float* A, float* U, float* S, float* V, long long n, cudaStream_t s);
+void launch_svd3_backward(const float* gU, const float* gS, const float* gV, const float* U, const float* S,
+                          const float* V, float* gA, long long n, cudaStream_t s);
+
+}  // namespace dstir

@@ -1,0 +1,814 @@
+// Forward and adjoint kernels of one MLS-MPM substep (sm_103a).
+//
+// Forward substep f (reference forward(s), simulation_functions.py:341-348):
+//   p2g_kernel   compute_F_tmp :39-42 + p2g :104-196 (stress, F[f+1], APIC scatter)
+//   grid_kernel  grid_op :199-225 (+ moving cylinder rod and its reaction force)
+//   g2p_kernel   g2p :228-290 (+ rod reaction force of compute_loss :330-336)
+// clear_grid (:3-10) is fused into grid_kernel (it zeroes the P2G grid after
+// reading it).  The reference's svd kernel (:55-58) feeds nothing downstream;
+// it runs here only when J is taken from the SVD (DSTIR_J_SVD).
+//
+// Adjoint substep f (the .grad kernels Taichi generated, called in reverse by
+// backward(s), :351-365): g2p_adj_kernel (G2P^T: scatter into the grid
+// adjoint), grid_adj_kernel (grid_op^T), p2g_adj_kernel (P2G^T: gather, stress
+// and F_tmp adjoints, parameter gradient block reduction).
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "internal.h"
+#include "svd.cuh"
+
+namespace dstir {
+
+// ---------------------------------------------------------------------------
+// reductions
+// ---------------------------------------------------------------------------
+template <int NV>
+__device__ __forceinline__ void block_reduce(float (&v)[NV], float (*sh)[4]) {
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) v[c] += __shfl_down_sync(0xffffffffu, v[c], off);
+    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) sh[warp][c] = v[c];
+    __syncthreads();
+    if (warp == 0) {
+        int nw = blockDim.x >> 5;
+#pragma unroll
+        for (int c = 0; c < NV; ++c) v[c] = lane < nw ? sh[lane][c] : 0.f;
+#pragma unroll
+        for (int off = 16; off > 0; off >>= 1)
+#pragma unroll
+            for (int c = 0; c < NV; ++c) v[c] += __shfl_down_sync(0xffffffffu, v[c], off);
+    }
+}
+
+// Every block of a (scene, purpose) group publishes its partial sum; the block
+// that arrives last adds the partials of the group in block order (so the
+// result does not depend on scheduling) and writes it to out[0..NV).
+template <int NV>
+__device__ __forceinline__ void group_sum(float (&v)[NV], float (*sh)[4], float* partial, unsigned* counter,
+                                          int group_first, int group_count, float* out, float scale) {
+    __shared__ bool is_last;
+    block_reduce<NV>(v, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) partial[(long long)blockIdx.x * 4 + c] = v[c];
+        __threadfence();
+        unsigned prev = atomicAdd(counter, 1u);
+        is_last = (prev == (unsigned)(group_count - 1));
+    }
+    __syncthreads();
+    if (!is_last) return;
+    __threadfence();
+    float acc[NV];
+#pragma unroll
+    for (int c = 0; c < NV; ++c) acc[c] = 0.f;
+    const volatile float* vp = partial;
+    for (int b = threadIdx.x; b < group_count; b += blockDim.x)
+#pragma unroll
+        for (int c = 0; c < NV; ++c) acc[c] += vp[(long long)(group_first + b) * 4 + c];
+    block_reduce<NV>(acc, sh);
+    if (threadIdx.x == 0) {
+#pragma unroll
+        for (int c = 0; c < NV; ++c) out[c] = acc[c] * scale;
+        *counter = 0u;
+    }
+}
+
+__device__ __forceinline__ void red_add4(float4* p, float a, float b, float c, float d) {
+    atomicAdd(p, make_float4(a, b, c, d));
+}
+
+// ---------------------------------------------------------------------------
+// state loads
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void load3(const float* st, long long stride, int o, long long p, float* v) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] = __ldg(st + (long long)(o + c) * stride + p);
+}
+__device__ __forceinline__ void load9(const float* st, long long stride, int o, long long p, float* v) {
+#pragma unroll
+    for (int c = 0; c < 9; ++c) v[c] = __ldg(st + (long long)(o + c) * stride + p);
+}
+__device__ __forceinline__ void store3(float* st, long long stride, int o, long long p, const float* v) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) st[(long long)(o + c) * stride + p] = v[c];
+}
+__device__ __forceinline__ void store9(float* st, long long stride, int o, long long p, const float* v) {
+#pragma unroll
+    for (int c = 0; c < 9; ++c) st[(long long)(o + c) * stride + p] = v[c];
+}
+
+// Stress and affine momentum of a liquid particle (p2g :111-152).
+struct LiquidP2G {
+    float Ft[9];
+    float A[9];
+    float vv[3];
+    float J;
+};
+
+__device__ __forceinline__ void liquid_p2g(const SceneDev& s, int model, const float* prm, const float* v,
+                                           const float* C, const float* F, LiquidP2G& o) {
+    float IC[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) IC[i] = s.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
+    matmul3(IC, F, o.Ft);
+    if (s.j_mode == DSTIR_J_SVD) {
+        float U[9], sg[3], V[9];
+        svd3(o.Ft, U, sg, V);
+        o.J = sg[0] * sg[1] * sg[2];
+    } else {
+        o.J = det3(o.Ft);
+    }
+    float nrm2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) nrm2 += C[i] * C[i];
+    float gamma = sqrtf(nrm2) + 1e-6f;
+    Visc vs = viscosity<false>(model, prm, gamma);
+    float pr = (s.bulk / 2.f) * (o.J - (1.f / o.J) - 1.f) * o.J;
+#pragma unroll
+    for (int a = 0; a < 3; ++a)
+#pragma unroll
+        for (int b = 0; b < 3; ++b) {
+            float Dab = 0.5f * (C[a * 3 + b] + C[b * 3 + a]);
+            float sig = vs.eta * Dab + ((a == b) ? pr : 0.f);
+            o.A[a * 3 + b] = s.alpha * sig + s.m_liq * C[a * 3 + b];
+        }
+    o.vv[0] = v[0];
+    o.vv[1] = v[1] + s.dt * s.gravity;
+    o.vv[2] = v[2];
+}
+
+// ---------------------------------------------------------------------------
+// forward
+// ---------------------------------------------------------------------------
+template <int VARIANT>
+__global__ void __launch_bounds__(256) p2g_kernel(FwdArgs a) {
+    __shared__ SceneDev s;
+    __shared__ BlockInfo bi;
+    if (threadIdx.x == 0) {
+        bi = a.blk[blockIdx.x];
+        s = a.sc[bi.scene];
+    }
+    __syncthreads();
+    long long p = bi.start + threadIdx.x;
+    if (p >= bi.end) return;
+    float x[3], v[3], C[9];
+    load3(a.cur, a.stride, OX, p, x);
+    load3(a.cur, a.stride, OV, p, v);
+    load9(a.cur, a.stride, OC, p, C);
+    float m, vv[3], A[9];
+    if (bi.kind == KIND_LIQUID) {
+        float F[9], prm[4];
+        load9(a.cur, a.stride, OF, p, F);
+#pragma unroll
+        for (int i = 0; i < 4; ++i) prm[i] = __ldg(a.params + bi.scene * 4 + i);
+        LiquidP2G q;
+        liquid_p2g(s, __ldg(a.models + bi.scene), prm, v, C, F, q);
+        store9(a.next, a.stride, OF, p, q.Ft);  // F[f+1] = F_tmp (:153)
+        m = s.m_liq;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = q.A[i];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vv[c] = q.vv[c];
+    } else {
+        float F[9];
+        load9(a.cur, a.stride, OF, p, F);
+        store9(a.next, a.stride, OF, p, F);
+        m = (bi.kind == KIND_ROD) ? s.m_rod : s.m_cont;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = m * C[i];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vv[c] = v[c];
+    }
+    int base[3];
+    float fx[3];
+    if (!locate(x, s.inv_dx, s.n, base, fx)) {
+        atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
+        return;
+    }
+    float w[3][3];
+    bspline(fx, w);
+    float mv[3] = {m * vv[0], m * vv[1], m * vv[2]};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            float wij = w[i][0] * w[j][1];
+            long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                float W = wij * w[k][2];
+                float dp0 = ((float)i - fx[0]) * s.dx, dp1 = ((float)j - fx[1]) * s.dx,
+                      dp2 = ((float)k - fx[2]) * s.dx;
+                float g0 = W * (mv[0] + (A[0] * dp0 + A[1] * dp1 + A[2] * dp2));
+                float g1 = W * (mv[1] + (A[3] * dp0 + A[4] * dp1 + A[5] * dp2));
+                float g2 = W * (mv[2] + (A[6] * dp0 + A[7] * dp1 + A[8] * dp2));
+                float gm = W * m;
+                float4* dst = a.pm + row + k;
+                if (VARIANT == P2G_PLAIN) {
+                    float* d = reinterpret_cast<float*>(dst);
+                    atomicAdd(d + 0, g0);
+                    atomicAdd(d + 1, g1);
+                    atomicAdd(d + 2, g2);
+                    atomicAdd(d + 3, gm);
+                } else {
+                    red_add4(dst, g0, g1, g2, gm);
+                }
+            }
+        }
+}
+
+__global__ void __launch_bounds__(256) grid_kernel(FwdArgs a) {
+    __shared__ SceneDev s;
+    __shared__ GridBlock gb;
+    __shared__ float sh[32][4];
+    __shared__ float rc[3], rodv[3];
+    if (threadIdx.x == 0) {
+        gb = a.gblk[blockIdx.x];
+        s = a.sc[gb.scene];
+        const float* t0 = a.traj + ((long long)gb.scene * a.traj_len + a.f) * 3;
+        for (int c = 0; c < 3; ++c) {
+            rc[c] = t0[c];
+            rodv[c] = (t0[3 + c] - t0[c]) / s.dt;
+        }
+    }
+    __syncthreads();
+    long long node = gb.start + threadIdx.x;
+    float fsum[3] = {0.f, 0.f, 0.f};
+    if (node < gb.end) {
+        long long local = node - s.goff;
+        int n = s.n;
+        int i = (int)(local / ((long long)n * n)), j = (int)((local / n) % n), k = (int)(local % n);
+        float4 g = a.pm[node];
+        if (a.clear_pm) a.pm[node] = make_float4(0.f, 0.f, 0.f, 0.f);
+        float inv_m = 1.f / (g.w + 1e-10f);
+        float v[3] = {inv_m * g.x, inv_m * g.y, inv_m * g.z};
+        if (s.container_wall) {  // :204-210
+            float d0 = (float)i * s.dx - s.ccx, d2 = (float)k * s.dx - s.ccz;
+            float n2 = d0 * d0 + d2 * d2;
+            if (n2 > s.cr2) {
+                float inv = 1.f / sqrtf(n2);
+                float u0 = d0 * inv, u2 = d2 * inv;
+                float dot = v[0] * u0 + v[2] * u2;
+                v[0] -= u0 * dot;
+                v[2] -= u2 * dot;
+            }
+        }
+        int b = s.bound;  // :211-224
+        if (i < b && v[0] < 0.f) v[0] = 0.f;
+        if (i > n - b && v[0] > 0.f) v[0] = 0.f;
+        if (k < b && v[2] < 0.f) v[2] = 0.f;
+        if (k > n - b && v[2] > 0.f) v[2] = 0.f;
+        if (j < b && v[1] < 0.f) v[1] = 0.f;
+        if (j > n - b && v[1] > 0.f) v[0] = v[1] = v[2] = 0.f;
+        if (s.rod_mode == DSTIR_ROD_CYLINDER) {
+            float ex = (float)i * s.dx - rc[0], ez = (float)k * s.dx - rc[2];
+            if (ex * ex + ez * ez < s.rod_r2 && (float)j * s.dx >= rc[1]) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) {
+                    float u = inv_m * (c == 0 ? g.x : (c == 1 ? g.y : g.z));
+                    fsum[c] = g.w * (rodv[c] - u) / s.dt;
+                    v[c] = rodv[c];
+                }
+            }
+        }
+        a.vo[node] = make_float4(v[0], v[1], v[2], 0.f);
+    }
+    if (s.rod_mode == DSTIR_ROD_CYLINDER) {
+        group_sum<3>(fsum, sh, a.partial, a.counters + gb.scene, blockIdx.x - gb.idx, gb.count,
+                     a.force + gb.scene * a.force_stride + (long long)a.fo * 3, 1.f);
+    }
+}
+
+__global__ void __launch_bounds__(256) g2p_kernel(FwdArgs a) {
+    __shared__ SceneDev s;
+    __shared__ BlockInfo bi;
+    __shared__ float sh[32][4];
+    __shared__ float tv[3];
+    if (threadIdx.x == 0) {
+        bi = a.blk[blockIdx.x];
+        s = a.sc[bi.scene];
+        const float* t0 = a.traj + ((long long)bi.scene * a.traj_len + a.f) * 3;
+        for (int c = 0; c < 3; ++c) tv[c] = (t0[3 + c] - t0[c]) / s.dt;
+    }
+    __syncthreads();
+    long long p = bi.start + threadIdx.x;
+    bool active = p < bi.end;
+    float dv[3] = {0.f, 0.f, 0.f};
+    if (active) {
+        float x[3];
+        load3(a.cur, a.stride, OX, p, x);
+        int base[3];
+        float fx[3];
+        float nv[3] = {0.f, 0.f, 0.f};
+        float nC[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) nC[i] = 0.f;
+        if (locate(x, s.inv_dx, s.n, base, fx)) {
+            float w[3][3];
+            bspline(fx, w);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    float wij = w[i][0] * w[j][1];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        float4 g = __ldg(a.vo + row + k);
+                        float W = wij * w[k][2];
+                        float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
+                        float wg0 = W * g.x, wg1 = W * g.y, wg2 = W * g.z;
+                        nv[0] += wg0;
+                        nv[1] += wg1;
+                        nv[2] += wg2;
+                        nC[0] += wg0 * d0; nC[1] += wg0 * d1; nC[2] += wg0 * d2;
+                        nC[3] += wg1 * d0; nC[4] += wg1 * d1; nC[5] += wg1 * d2;
+                        nC[6] += wg2 * d0; nC[7] += wg2 * d1; nC[8] += wg2 * d2;
+                    }
+                }
+            float c4 = 4.f * s.inv_dx;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) nC[i] *= c4;
+        } else {
+            atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
+        }
+        store9(a.next, a.stride, OC, p, nC);
+        float nx[3], outv[3];
+        if (bi.kind == KIND_LIQUID) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                outv[c] = nv[c];
+                nx[c] = x[c] + s.dt * nv[c];
+            }
+            bool fin = isfinite(nx[0]) && isfinite(nx[1]) && isfinite(nx[2]) && isfinite(nv[0]) &&
+                       isfinite(nv[1]) && isfinite(nv[2]);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) fin = fin && isfinite(nC[i]);
+            if (!fin) atomicOr(a.status, DSTIR_STATUS_NAN);
+        } else if (bi.kind == KIND_ROD) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                dv[c] = tv[c] - nv[c];  // :267
+                outv[c] = tv[c];
+                nx[c] = x[c] + tv[c] * s.dt;
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                outv[c] = 0.f;
+                nx[c] = x[c];
+            }
+        }
+        store3(a.next, a.stride, OV, p, outv);
+        store3(a.next, a.stride, OX, p, nx);
+    }
+    if (bi.kind == KIND_ROD && s.rod_mode == DSTIR_ROD_PARTICLES) {
+        group_sum<3>(dv, sh, a.partial, a.counters + a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,
+                     a.force + bi.scene * a.force_stride + (long long)a.fo * 3, s.force_scale);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// adjoint
+// ---------------------------------------------------------------------------
+template <int VARIANT>
+__global__ void __launch_bounds__(256) g2p_adj_kernel(AdjArgs a) {
+    __shared__ SceneDev s;
+    __shared__ BlockInfo bi;
+    __shared__ float fb[3];
+    if (threadIdx.x == 0) {
+        bi = a.blk[blockIdx.x];
+        s = a.sc[bi.scene];
+        const float* d = a.dforce + bi.scene * a.dforce_stride + (long long)a.fo * 3;
+        for (int c = 0; c < 3; ++c) fb[c] = d[c];
+    }
+    __syncthreads();
+    long long p = bi.start + threadIdx.x;
+    if (p >= bi.end) return;
+    float x[3];
+    load3(a.cur, a.stride, OX, p, x);
+    float xb[3] = {0.f, 0.f, 0.f}, vnb[3], Cb[9];
+    load9(a.adj_next, a.stride, OC, p, Cb);
+    if (bi.kind == KIND_LIQUID) {
+        float ax[3], av[3];
+        load3(a.adj_next, a.stride, OX, p, ax);
+        load3(a.adj_next, a.stride, OV, p, av);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            vnb[c] = av[c] + s.dt * ax[c];  // x[f+1] = x[f] + dt*v[f+1] (:247)
+            xb[c] = ax[c];
+        }
+    } else if (bi.kind == KIND_ROD && s.rod_mode == DSTIR_ROD_PARTICLES) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vnb[c] = -fb[c] * s.force_scale;  // dv = v_pres - v_grid
+    } else {
+        vnb[0] = vnb[1] = vnb[2] = 0.f;
+    }
+    int base[3];
+    float fx[3];
+    if (locate(x, s.inv_dx, s.n, base, fx)) {
+        float w[3][3], dw[3][3];
+        bspline_d(fx, w, dw);
+        float c4 = 4.f * s.inv_dx;
+        float fxb[3] = {0.f, 0.f, 0.f};
+        const bool liquid = bi.kind == KIND_LIQUID;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    float W = w[i][0] * w[j][1] * w[k][2];
+                    float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
+                    float Cd0 = Cb[0] * d0 + Cb[1] * d1 + Cb[2] * d2;
+                    float Cd1 = Cb[3] * d0 + Cb[4] * d1 + Cb[5] * d2;
+                    float Cd2 = Cb[6] * d0 + Cb[7] * d1 + Cb[8] * d2;
+                    float4* dst = a.ga + row + k;
+                    float g0 = W * (vnb[0] + c4 * Cd0), g1 = W * (vnb[1] + c4 * Cd1), g2 = W * (vnb[2] + c4 * Cd2);
+                    if (VARIANT == P2G_PLAIN) {
+                        float* dd = reinterpret_cast<float*>(dst);
+                        atomicAdd(dd + 0, g0);
+                        atomicAdd(dd + 1, g1);
+                        atomicAdd(dd + 2, g2);
+                    } else {
+                        red_add4(dst, g0, g1, g2, 0.f);
+                    }
+                    if (liquid) {
+                        float4 g = __ldg(a.vo + row + k);
+                        float Wb = vnb[0] * g.x + vnb[1] * g.y + vnb[2] * g.z +
+                                   c4 * (g.x * Cd0 + g.y * Cd1 + g.z * Cd2);
+                        // C_new depends on fx through dp = o - fx
+                        fxb[0] -= c4 * W * (Cb[0] * g.x + Cb[3] * g.y + Cb[6] * g.z);
+                        fxb[1] -= c4 * W * (Cb[1] * g.x + Cb[4] * g.y + Cb[7] * g.z);
+                        fxb[2] -= c4 * W * (Cb[2] * g.x + Cb[5] * g.y + Cb[8] * g.z);
+                        fxb[0] += Wb * dw[i][0] * w[j][1] * w[k][2];
+                        fxb[1] += Wb * w[i][0] * dw[j][1] * w[k][2];
+                        fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
+                    }
+                }
+            }
+        if (liquid)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
+    }
+    if (bi.kind == KIND_LIQUID) store3(a.adj_cur, a.stride, OX, p, xb);
+}
+
+__global__ void __launch_bounds__(256) grid_adj_kernel(AdjArgs a) {
+    __shared__ SceneDev s;
+    __shared__ GridBlock gb;
+    __shared__ float rc[3], rodv[3], fb[3];
+    if (threadIdx.x == 0) {
+        gb = a.gblk[blockIdx.x];
+        s = a.sc[gb.scene];
+        const float* t0 = a.traj + ((long long)gb.scene * a.traj_len + a.f) * 3;
+        const float* d = a.dforce + gb.scene * a.dforce_stride + (long long)a.fo * 3;
+        for (int c = 0; c < 3; ++c) {
+            rc[c] = t0[c];
+            rodv[c] = (t0[3 + c] - t0[c]) / s.dt;
+            fb[c] = d[c];
+        }
+    }
+    __syncthreads();
+    long long node = gb.start + threadIdx.x;
+    if (node >= gb.end) return;
+    long long local = node - s.goff;
+    int n = s.n;
+    int i = (int)(local / ((long long)n * n)), j = (int)((local / n) % n), k = (int)(local % n);
+    float4 g = a.pm[node];
+    float4 vb4 = a.ga[node];
+    a.ga[node] = make_float4(0.f, 0.f, 0.f, 0.f);
+    float inv_m = 1.f / (g.w + 1e-10f);
+    float u[3] = {inv_m * g.x, inv_m * g.y, inv_m * g.z};
+    float v[3] = {u[0], u[1], u[2]};
+    bool proj = false;
+    float u0 = 0.f, u2 = 0.f;
+    if (s.container_wall) {
+        float d0 = (float)i * s.dx - s.ccx, d2 = (float)k * s.dx - s.ccz;
+        float n2 = d0 * d0 + d2 * d2;
+        if (n2 > s.cr2) {
+            float inv = 1.f / sqrtf(n2);
+            u0 = d0 * inv;
+            u2 = d2 * inv;
+            float dot = v[0] * u0 + v[2] * u2;
+            v[0] -= u0 * dot;
+            v[2] -= u2 * dot;
+            proj = true;
+        }
+    }
+    float mask[3] = {1.f, 1.f, 1.f};
+    int b = s.bound;
+    if (i < b && v[0] < 0.f) { v[0] = 0.f; mask[0] = 0.f; }
+    if (i > n - b && v[0] > 0.f) { v[0] = 0.f; mask[0] = 0.f; }
+    if (k < b && v[2] < 0.f) { v[2] = 0.f; mask[2] = 0.f; }
+    if (k > n - b && v[2] > 0.f) { v[2] = 0.f; mask[2] = 0.f; }
+    if (j < b && v[1] < 0.f) { v[1] = 0.f; mask[1] = 0.f; }
+    if (j > n - b && v[1] > 0.f) { mask[0] = mask[1] = mask[2] = 0.f; }
+    bool inside = false;
+    if (s.rod_mode == DSTIR_ROD_CYLINDER) {
+        float ex = (float)i * s.dx - rc[0], ez = (float)k * s.dx - rc[2];
+        inside = (ex * ex + ez * ez < s.rod_r2 && (float)j * s.dx >= rc[1]);
+    }
+    float ub[3], mb = 0.f;
+    if (inside) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            ub[c] = -g.w * fb[c] / s.dt;
+            mb += fb[c] * (rodv[c] - u[c]) / s.dt;
+        }
+    } else {
+        ub[0] = mask[0] * vb4.x;
+        ub[1] = mask[1] * vb4.y;
+        ub[2] = mask[2] * vb4.z;
+        if (proj) {
+            float dot = ub[0] * u0 + ub[2] * u2;
+            ub[0] -= u0 * dot;
+            ub[2] -= u2 * dot;
+        }
+    }
+    float Pu = g.x * ub[0] + g.y * ub[1] + g.z * ub[2];
+    a.pmb[node] = make_float4(inv_m * ub[0], inv_m * ub[1], inv_m * ub[2], mb - inv_m * inv_m * Pu);
+}
+
+__global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
+    __shared__ SceneDev s;
+    __shared__ BlockInfo bi;
+    __shared__ float sh[32][4];
+    if (threadIdx.x == 0) {
+        bi = a.blk[blockIdx.x];
+        s = a.sc[bi.scene];
+    }
+    __syncthreads();
+    long long p = bi.start + threadIdx.x;
+    bool active = p < bi.end;
+    float pg[4] = {0.f, 0.f, 0.f, 0.f};
+    if (active) {
+        float x[3], v[3], C[9];
+        load3(a.cur, a.stride, OX, p, x);
+        load3(a.cur, a.stride, OV, p, v);
+        load9(a.cur, a.stride, OC, p, C);
+        const bool liquid = bi.kind == KIND_LIQUID;
+        float m, vv[3], A[9];
+        float F[9], IC[9], Ft[9], J = 1.f, nrm = 0.f, pr = 0.f;
+        float U[9], sg[3], Vm[9];
+        float prm[4];
+        Visc vs;
+        vs.eta = 0.f;
+        int model = 0;
+        if (liquid) {
+            load9(a.cur, a.stride, OF, p, F);
+#pragma unroll
+            for (int i = 0; i < 4; ++i) prm[i] = __ldg(a.params + bi.scene * 4 + i);
+            model = __ldg(a.models + bi.scene);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) IC[i] = s.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
+            matmul3(IC, F, Ft);
+            if (s.j_mode == DSTIR_J_SVD) {
+                svd3(Ft, U, sg, Vm);
+                J = sg[0] * sg[1] * sg[2];
+            } else {
+                J = det3(Ft);
+            }
+            float nrm2 = 0.f;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) nrm2 += C[i] * C[i];
+            nrm = sqrtf(nrm2);
+            vs = viscosity<true>(model, prm, nrm + 1e-6f);
+            pr = (s.bulk / 2.f) * (J - (1.f / J) - 1.f) * J;
+            m = s.m_liq;
+#pragma unroll
+            for (int aa = 0; aa < 3; ++aa)
+#pragma unroll
+                for (int bb = 0; bb < 3; ++bb) {
+                    float Dab = 0.5f * (C[aa * 3 + bb] + C[bb * 3 + aa]);
+                    A[aa * 3 + bb] = s.alpha * (vs.eta * Dab + ((aa == bb) ? pr : 0.f)) + m * C[aa * 3 + bb];
+                }
+            vv[0] = v[0];
+            vv[1] = v[1] + s.dt * s.gravity;
+            vv[2] = v[2];
+        } else {
+            m = (bi.kind == KIND_ROD) ? s.m_rod : s.m_cont;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) A[i] = m * C[i];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) vv[c] = v[c];
+        }
+        float Ab[9], vvb[3] = {0.f, 0.f, 0.f}, fxb[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Ab[i] = 0.f;
+        int base[3];
+        float fx[3];
+        if (locate(x, s.inv_dx, s.n, base, fx)) {
+            float w[3][3], dw[3][3];
+            bspline_d(fx, w, dw);
+            float mv[3] = {m * vv[0], m * vv[1], m * vv[2]};
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        float4 gb = __ldg(a.pmb + row + k);
+                        float W = w[i][0] * w[j][1] * w[k][2];
+                        float dp[3] = {((float)i - fx[0]) * s.dx, ((float)j - fx[1]) * s.dx,
+                                       ((float)k - fx[2]) * s.dx};
+                        float gbv[3] = {gb.x, gb.y, gb.z};
+                        float Wb = gb.w * m;
+#pragma unroll
+                        for (int aa = 0; aa < 3; ++aa) {
+                            float ad = A[aa * 3 + 0] * dp[0] + A[aa * 3 + 1] * dp[1] + A[aa * 3 + 2] * dp[2];
+                            Wb += gbv[aa] * (mv[aa] + ad);
+                            vvb[aa] += W * m * gbv[aa];
+#pragma unroll
+                            for (int bb = 0; bb < 3; ++bb) Ab[aa * 3 + bb] += W * gbv[aa] * dp[bb];
+                        }
+                        if (liquid) {
+#pragma unroll
+                            for (int bb = 0; bb < 3; ++bb)
+                                fxb[bb] -= W * s.dx *
+                                           (A[0 * 3 + bb] * gbv[0] + A[1 * 3 + bb] * gbv[1] + A[2 * 3 + bb] * gbv[2]);
+                            fxb[0] += Wb * dw[i][0] * w[j][1] * w[k][2];
+                            fxb[1] += Wb * w[i][0] * dw[j][1] * w[k][2];
+                            fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
+                        }
+                    }
+                }
+        }
+        float Cb[9];
+        if (!liquid) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Cb[i] = m * Ab[i];
+            float z[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) z[i] = 0.f;
+            store3(a.adj_cur, a.stride, OX, p, z);
+            store3(a.adj_cur, a.stride, OV, p, z);
+            store9(a.adj_cur, a.stride, OC, p, Cb);
+            store9(a.adj_cur, a.stride, OF, p, z);
+        } else {
+            float xb[3];
+            load3(a.adj_cur, a.stride, OX, p, xb);  // G2P part, written by g2p_adj_kernel
+#pragma unroll
+            for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
+            store3(a.adj_cur, a.stride, OX, p, xb);
+            store3(a.adj_cur, a.stride, OV, p, vvb);
+            float sigb[9];
+#pragma unroll
+            for (int i = 0; i < 9; ++i) {
+                Cb[i] = m * Ab[i];
+                sigb[i] = s.alpha * Ab[i];
+            }
+            float etab = 0.f;
+#pragma unroll
+            for (int aa = 0; aa < 3; ++aa)
+#pragma unroll
+                for (int bb = 0; bb < 3; ++bb) {
+                    float Dab = 0.5f * (C[aa * 3 + bb] + C[bb * 3 + aa]);
+                    etab += sigb[aa * 3 + bb] * Dab;
+                    Cb[aa * 3 + bb] += vs.eta * 0.5f * (sigb[aa * 3 + bb] + sigb[bb * 3 + aa]);
+                }
+            float trb = sigb[0] + sigb[4] + sigb[8];
+            float Jb = trb * (s.bulk / 2.f) * (2.f * J - 1.f);
+            float Ftb[9];
+            load9(a.adj_next, a.stride, OF, p, Ftb);  // F[f+1] = F_tmp
+            if (s.j_mode == DSTIR_J_SVD) {
+                float gS[3] = {Jb * sg[1] * sg[2], Jb * sg[0] * sg[2], Jb * sg[0] * sg[1]};
+                float z[9], gA[9];
+#pragma unroll
+                for (int i = 0; i < 9; ++i) z[i] = 0.f;
+                svd3_backward(z, gS, z, U, sg, Vm, gA);
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Ftb[i] += gA[i];
+            } else {
+                float cf[9];
+                cof3(Ft, cf);
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Ftb[i] += Jb * cf[i];
+            }
+            float gammab = etab * vs.deta_dgamma;
+#pragma unroll
+            for (int i = 0; i < 4; ++i) pg[i] = etab * vs.dp[i];
+            if (nrm > 0.f) {
+                float inv = gammab / nrm;
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Cb[i] += inv * C[i];
+            }
+            float Fb[9];
+#pragma unroll
+            for (int aa = 0; aa < 3; ++aa)
+#pragma unroll
+                for (int bb = 0; bb < 3; ++bb) {
+                    float sF = 0.f, sC = 0.f;
+#pragma unroll
+                    for (int c = 0; c < 3; ++c) {
+                        sF += IC[c * 3 + aa] * Ftb[c * 3 + bb];
+                        sC += Ftb[aa * 3 + c] * F[bb * 3 + c];
+                    }
+                    Fb[aa * 3 + bb] = sF;
+                    Cb[aa * 3 + bb] += s.dt * sC;
+                }
+            store9(a.adj_cur, a.stride, OC, p, Cb);
+            store9(a.adj_cur, a.stride, OF, p, Fb);
+        }
+    }
+    if (bi.kind == KIND_LIQUID) {
+        group_sum<4>(pg, sh, a.partial, a.counters + 2 * a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,
+                     a.pgrad + ((long long)a.fo * a.batch + bi.scene) * 4, 1.f);
+    }
+}
+
+// ---------------------------------------------------------------------------
+// layout and reduction helpers
+// ---------------------------------------------------------------------------
+__global__ void pack_state_kernel(const float* x, const float* v, const float* C, const float* F, float* st,
+                                  long long stride, long long n) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        st[(OX + c) * stride + p] = x[p * 3 + c];
+        st[(OV + c) * stride + p] = v ? v[p * 3 + c] : 0.f;
+    }
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+        st[(OC + c) * stride + p] = C ? C[p * 9 + c] : 0.f;
+        st[(OF + c) * stride + p] = F ? F[p * 9 + c] : ((c % 4 == 0) ? 1.f : 0.f);
+    }
+}
+
+__global__ void unpack_state_kernel(const float* st, long long stride, long long n, float* x, float* v, float* C,
+                                    float* F) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p >= n) return;
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        if (x) x[p * 3 + c] = st[(OX + c) * stride + p];
+        if (v) v[p * 3 + c] = st[(OV + c) * stride + p];
+    }
+#pragma unroll
+    for (int c = 0; c < 9; ++c) {
+        if (C) C[p * 9 + c] = st[(OC + c) * stride + p];
+        if (F) F[p * 9 + c] = st[(OF + c) * stride + p];
+    }
+}
+
+// out[b*4+c] = sum_t pgrad[(t*B+b)*4+c], one block per (b, c), fixed order
+__global__ void reduce_pgrad_kernel(const float* pgrad, int T, int B, float* out) {
+    __shared__ float sh[32][4];
+    int b = blockIdx.x >> 2, c = blockIdx.x & 3;
+    float acc[1] = {0.f};
+    for (int t = threadIdx.x; t < T; t += blockDim.x) acc[0] += pgrad[((long long)t * B + b) * 4 + c];
+    block_reduce<1>(acc, sh);
+    if (threadIdx.x == 0) out[b * 4 + c] = acc[0];
+}
+
+// ---------------------------------------------------------------------------
+// launchers
+// ---------------------------------------------------------------------------
+void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, cudaStream_t st) {
+    if (n_blocks <= 0) return;
+    if (variant == P2G_PLAIN)
+        p2g_kernel<P2G_PLAIN><<<n_blocks, block, 0, st>>>(a);
+    else
+        p2g_kernel<P2G_VEC><<<n_blocks, block, 0, st>>>(a);
+}
+void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
+    if (n_gblocks > 0) grid_kernel<<<n_gblocks, gblock, 0, st>>>(a);
+}
+void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st) {
+    if (n_blocks > 0) g2p_kernel<<<n_blocks, block, 0, st>>>(a);
+}
+void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st) {
+    if (n_blocks <= 0) return;
+    if (variant == P2G_PLAIN)
+        g2p_adj_kernel<P2G_PLAIN><<<n_blocks, block, 0, st>>>(a);
+    else
+        g2p_adj_kernel<P2G_VEC><<<n_blocks, block, 0, st>>>(a);
+}
+void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
+    if (n_gblocks > 0) grid_adj_kernel<<<n_gblocks, gblock, 0, st>>>(a);
+}
+void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, cudaStream_t st) {
+    if (n_blocks > 0) p2g_adj_kernel<<<n_blocks, block, 0, st>>>(a);
+}
+void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
+                       long long stride, long long n, cudaStream_t s) {
+    if (n > 0) pack_state_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, v, C, F, st, stride, n);
+}
+void launch_unpack_state(const float* st, long long stride, long long n, float* x, float* v, float* C,
+                         float* F, cudaStream_t s) {
+    if (n > 0) unpack_state_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st, stride, n, x, v, C, F);
+}
+void launch_reduce_pgrad(const float* pgrad, int T, int B, float* out, cudaStream_t s) {
+    if (B > 0) reduce_pgrad_kernel<<<B * 4, 256, 0, s>>>(pgrad, T, B, out);
+}
+
+}  // namespace dstir

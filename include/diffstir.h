@@ -1,0 +1,161 @@
+/*
+ * diffstir.h - C ABI of the GB300 (sm_103a) differentiable MLS-MPM stirring
+ * simulator.
+ *
+ * The reference (denzelzheng/DiffStir) is a Python/Taichi program with no FFI
+ * of its own: its callers (src/gradient_descent_module.py,
+ * src/force_calculation_and_animation_module.py) drive the module-level
+ * Taichi kernels of src/simulator/simulation_functions.py.  Every entry point
+ * below replaces one group of those kernels or one of the field accesses the
+ * callers make; the reference line each one stands in for is cited beside it.
+ * The Python package diffstir_gb300 (ctypes) binds exactly these symbols.
+ *
+ * Conventions
+ *  - All float / int pointers passed to compute entry points are DEVICE
+ *    pointers owned by the caller (for instance torch CUDA tensors), unless a
+ *    parameter says "host".
+ *  - `stream` is a cudaStream_t passed as void*; NULL means the legacy default
+ *    stream.  A handle may be used from one host thread at a time.
+ *  - Return value: DSTIR_OK (0) or a negative DSTIR_E* code; the message of the
+ *    last failure is kept per handle (dstir_last_error).  No C++ exception
+ *    crosses this boundary.
+ *  - Particle order inside a handle is scene-major and, inside a scene,
+ *    [liquid | rod | container], with counts from DstirSceneDesc.
+ */
+#ifndef DIFFSTIR_H
+#define DIFFSTIR_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define DSTIR_OK 0
+#define DSTIR_EINVAL (-1)   /* bad argument */
+#define DSTIR_ENOMEM (-2)   /* device allocation failed */
+#define DSTIR_ECUDA (-3)    /* a CUDA call failed */
+#define DSTIR_ESTATE (-4)   /* call order, e.g. backward without a recorded forward */
+#define DSTIR_ERANGE (-5)   /* size beyond a fixed limit */
+
+/* bits of the device status word (dstir_status) */
+#define DSTIR_STATUS_NAN 1u          /* a non-finite particle state was produced */
+#define DSTIR_STATUS_OUT_OF_GRID 2u  /* a particle stencil left the grid; it was skipped */
+
+/* viscosity models: src/simulator/simulation_functions.py:118-146 */
+#define DSTIR_MODEL_CARREAU 0   /* params [eta0, eta_inf, n, lambda] */
+#define DSTIR_MODEL_CROSS 1     /* params [eta0, eta_inf, n, lambda] */
+#define DSTIR_MODEL_HB 2        /* params [K, tau_y, n, unused]; power law = HB with tau_y 0 */
+
+/* rod representation */
+#define DSTIR_ROD_PARTICLES 0   /* kinematic rod particles, reference :165-180, :250-270 */
+#define DSTIR_ROD_CYLINDER 1    /* analytic moving cylinder in the grid update */
+
+/* J used by the bulk term */
+#define DSTIR_J_DET 0           /* J = det(F_tmp), reference :113 */
+#define DSTIR_J_SVD 1           /* J = s1*s2*s3 from the per-particle 3x3 SVD */
+
+/* One scene.  Field names follow src/simulator/initialization.py:14-54. */
+typedef struct DstirSceneDesc {
+    int32_t n_grid;          /* nodes per axis, dx = 1/n_grid (initialization.py:22-24) */
+    int32_t bound;           /* wall layers (initialization.py:15) */
+    int32_t n_liquid;        /* n_particles */
+    int32_t n_rod;           /* n_operator_particles (0 in cylinder mode) */
+    int32_t n_container;     /* n_container_particles */
+    int32_t model;           /* DSTIR_MODEL_* (model_index) */
+    int32_t rod_mode;        /* DSTIR_ROD_* */
+    int32_t j_mode;          /* DSTIR_J_* */
+    int32_t container_wall;  /* 1: cylindrical container projection in the grid update (:204-210) */
+    int32_t reserved;
+    float dt;                /* substep (arguments.json simulation_setting.dt) */
+    float gravity;           /* y acceleration added to liquid velocity in P2G (:152), -9.81*scale */
+    float bulk_modulus;      /* k of (k/2)(J-1/J-1)J (:112, 20000 in the reference) */
+    float liquid_p_vol;      /* liquid_p_vol */
+    float liquid_p_mass;     /* liquid_p_mass */
+    float rod_p_mass;        /* operator_p_mass */
+    float container_p_mass;  /* container_p_mass */
+    float force_scale;       /* particle rod: force = sum(dv) * force_scale (= V_o*rho_o/dt, :335-336) */
+    float container_cx;      /* container axis x (0.5 in the reference, :206) */
+    float container_cz;      /* container axis z (0.5) */
+    float container_r;       /* projection radius (0.0415 - dx/2, :205) */
+    float rod_radius;        /* cylinder mode: rod radius; the rod occupies y >= trajectory y */
+} DstirSceneDesc;
+
+typedef struct DstirHandle DstirHandle;
+
+/* Create a simulator for `batch` scenes able to run up to `max_steps`
+ * substeps per rollout.  Replaces the field allocation of
+ * src/simulator/initialization.py:123-165 (time-indexed fields become K-step
+ * checkpoints owned by the handle). */
+int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
+                 DstirHandle** out);
+void dstir_destroy(DstirHandle* h);
+const char* dstir_last_error(const DstirHandle* h);
+/* total particles (all scenes, all kinds) and scene count */
+int dstir_num_particles(const DstirHandle* h, int64_t* n_total, int32_t* batch);
+
+/* Upload the step-0 particle state, AoS: x,v [N,3], C,F [N,3,3] row-major.
+ * v/C may be NULL (zero) and F may be NULL (identity).  Replaces
+ * initialize_objects / initialize_ti_field, simulation_functions.py:293-319. */
+int dstir_set_state(DstirHandle* h, const float* x, const float* v, const float* C,
+                    const float* F, void* stream);
+/* Read the current particle state back, same layout (any pointer may be NULL).
+ * Replaces x/operator_x/container_x .to_numpy(), gradient_descent_module.py:131-132. */
+int dstir_get_state(DstirHandle* h, float* x, float* v, float* C, float* F, void* stream);
+
+/* params [batch,4] (constitutive_parameters, initialization.py:134), models
+ * [batch] or NULL to keep the scene descriptors' model (model_index). */
+int dstir_set_params(DstirHandle* h, const float* params, const int32_t* models, void* stream);
+
+/* Rod reference-point trajectory [batch, max_steps+1, 3]; substep f uses
+ * entries f and f+1 (operator_kinematic_seq, simulation_functions.py:266;
+ * for the cylinder the point is (axis x, lowest y, axis z)). */
+int dstir_set_trajectory(DstirHandle* h, const float* traj, void* stream);
+
+/* Advance `nsteps` substeps starting at substep index t0 (which selects the
+ * trajectory entries).  force_out [batch, nsteps, 3] receives the rod reaction
+ * force of each substep: entry f is the reference's force at frame t0+f+1
+ * (compute_loss, :330-339).  With record != 0 the state is checkpointed every
+ * `ckpt_every` substeps for dstir_backward.  Replaces forward(s), :341-348. */
+int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every,
+                  int32_t record, float* force_out, void* stream);
+
+/* One substep without recording (the reference's forward(s) called alone,
+ * src/force_calculation_and_animation_module.py:8-9). force_out [batch,3] or NULL. */
+int dstir_substep(DstirHandle* h, int32_t f, float* force_out, void* stream);
+
+/* Reverse pass of the last recorded dstir_forward: given dL/dforce
+ * [batch, nsteps, 3] it writes dL/dparams [batch,4] and optionally dL/d(step-0
+ * state) (x,v [N,3], C,F [N,9]; NULL to skip).  Segments are recomputed from
+ * the checkpoints.  Replaces backward(s) (:351-365) driven by ti.ad.Tape
+ * (gradient_descent_module.py:103-107) and constitutive_parameters.grad. */
+int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams,
+                   float* dL_dx0, float* dL_dv0, float* dL_dC0, float* dL_dF0,
+                   void* stream);
+
+/* OR of DSTIR_STATUS_* raised on the device since the last call; clears it.
+ * Synchronises `stream`.  (The reference only prints NaNs,
+ * gradient_descent_module.py:51-54.) */
+int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
+
+/* Tuning knobs: "p2g" (0 plain scalar atomics, 1 vector atomics, 2 binned
+ * shared-memory tiles), "block" (threads per block), "graph" (1: capture each
+ * checkpoint segment as a CUDA graph), "tile" (tile cells per CTA). */
+int dstir_set_option(DstirHandle* h, const char* key, int64_t value);
+int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value);
+
+/* Batched 3x3 SVD, A = U diag(S) V^T with det U = det V = +1 (the last
+ * singular value carries the sign of det A), A/U/V [n,3,3], S [n,3].
+ * Replaces the svd kernel (ti.svd), simulation_functions.py:55-58. */
+int dstir_svd3(const float* A, float* U, float* S, float* V, int64_t n, void* stream);
+/* SVD backward, simulation_functions.py:61-93 (backward_svd with the clamped
+ * 1/(s_j^2 - s_i^2) terms evaluated in FP64): gA = f(gU, gS, gV, U, S, V).
+ * gS is [n,3] (the diagonal of the reference's sig.grad). */
+int dstir_svd3_backward(const float* gU, const float* gS, const float* gV, const float* U,
+                        const float* S, const float* V, float* gA, int64_t n, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* DIFFSTIR_H */

@@ -1,0 +1,134 @@
+"""CPU oracle of the DiffStir MLS-MPM path (test infrastructure).
+
+Only tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference
+arm may import this package, and only as the checker or as the timed CPU
+stand-in for the reference; the diffstir_gb300 product never does.
+
+``build()`` compiles oracle.cpp (a line-by-line C++ restatement of
+src/simulator/simulation_functions.py with a hand-derived adjoint) into
+``oracle/_build/liboracle.so`` with g++ and OpenMP.
+"""
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+SRC = os.path.join(HERE, 'oracle.cpp')
+OUT_DIR = os.path.join(HERE, '_build')
+LIB = os.path.join(OUT_DIR, 'liboracle.so')
+
+_lib = None
+
+
+def build(force=False):
+    os.makedirs(OUT_DIR, exist_ok=True)
+    hdr = os.path.join(HERE, '..', 'include', 'diffstir.h')
+    if (not force and os.path.exists(LIB)
+            and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr))):
+        return LIB
+    tmp = LIB + '.tmp%d' % os.getpid()
+    cmd = ['g++', '-O2', '-std=c++17', '-fopenmp', '-fPIC', '-shared', '-o', tmp, SRC]
+    subprocess.run(cmd, check=True)
+    os.replace(tmp, LIB)
+    return LIB
+
+
+def load():
+    global _lib
+    if _lib is None:
+        from diffstir_gb300._abi import DstirSceneDesc
+        build()
+        lib = C.CDLL(LIB)
+        D = C.POINTER(C.c_double)
+        sig_roll = [C.POINTER(DstirSceneDesc), D, D, C.c_int, D, D, D, D, D, D, C.c_int]
+        sig_grad = [C.POINTER(DstirSceneDesc), D, D, C.c_int, D, D, D, D, D, D, D, D, C.c_int]
+        for name in ('oracle_rollout_f64', 'oracle_rollout_f32'):
+            getattr(lib, name).argtypes = sig_roll
+            getattr(lib, name).restype = C.c_int
+        for name in ('oracle_grad_f64', 'oracle_grad_f32'):
+            getattr(lib, name).argtypes = sig_grad
+            getattr(lib, name).restype = C.c_int
+        lib.oracle_svd3_f64.argtypes = [D, D, D, D, C.c_int64]
+        lib.oracle_svd3_f64.restype = None
+        lib.oracle_svd3_backward_f64.argtypes = [D, D, D, D, D, D, D, C.c_int64]
+        lib.oracle_svd3_backward_f64.restype = None
+        lib.oracle_max_threads.restype = C.c_int
+        _lib = lib
+    return _lib
+
+
+def _p(a):
+    if a is None:
+        return None
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _arr(a, shape=None):
+    if a is None:
+        return None
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+def rollout(desc, params, traj, T, x0, v0=None, C0=None, F0=None, precision='f64',
+            threads=1, return_states=False):
+    """Forward rollout; returns (force [T,3], states [(T+1),N,24] or None, status)."""
+    lib = load()
+    N = desc.n_liquid + desc.n_rod + desc.n_container
+    params, traj = _arr(params), _arr(traj)
+    x0, v0, C0, F0 = _arr(x0), _arr(v0), _arr(C0), _arr(F0)
+    force = np.zeros((T, 3))
+    states = np.zeros((T + 1, N, 24)) if return_states else None
+    fn = lib.oracle_rollout_f64 if precision == 'f64' else lib.oracle_rollout_f32
+    rc = fn(C.byref(desc), _p(params), _p(traj), T, _p(x0), _p(v0), _p(C0), _p(F0),
+            _p(force), _p(states), threads)
+    if rc < 0:
+        raise RuntimeError('oracle rollout failed: %d' % rc)
+    return force, states, rc
+
+
+def grad(desc, params, traj, T, x0, dL_dforce, v0=None, C0=None, F0=None, precision='f64',
+         threads=1, want_state0=False):
+    """Rollout + reverse pass; returns (force, dL_dparams[4], dL_dstate0 [N,24] or None, status)."""
+    lib = load()
+    N = desc.n_liquid + desc.n_rod + desc.n_container
+    params, traj = _arr(params), _arr(traj)
+    x0, v0, C0, F0 = _arr(x0), _arr(v0), _arr(C0), _arr(F0)
+    dL = _arr(dL_dforce, (T, 3))
+    force = np.zeros((T, 3))
+    dp = np.zeros(4)
+    ds = np.zeros((N, 24)) if want_state0 else None
+    fn = lib.oracle_grad_f64 if precision == 'f64' else lib.oracle_grad_f32
+    rc = fn(C.byref(desc), _p(params), _p(traj), T, _p(x0), _p(v0), _p(C0), _p(F0),
+            _p(dL), _p(force), _p(dp), _p(ds), threads)
+    if rc < 0:
+        raise RuntimeError('oracle grad failed: %d' % rc)
+    return force, dp, ds, rc
+
+
+def svd3(A):
+    lib = load()
+    A = _arr(A).reshape(-1, 9)
+    n = A.shape[0]
+    U, S, V = np.zeros((n, 9)), np.zeros((n, 3)), np.zeros((n, 9))
+    lib.oracle_svd3_f64(_p(A), _p(U), _p(S), _p(V), n)
+    return U.reshape(n, 3, 3), S, V.reshape(n, 3, 3)
+
+
+def svd3_backward(gU, gS, gV, U, S, V):
+    lib = load()
+    gU, gS, gV = _arr(gU).reshape(-1, 9), _arr(gS).reshape(-1, 3), _arr(gV).reshape(-1, 9)
+    U, S, V = _arr(U).reshape(-1, 9), _arr(S).reshape(-1, 3), _arr(V).reshape(-1, 9)
+    n = U.shape[0]
+    gA = np.zeros((n, 9))
+    lib.oracle_svd3_backward_f64(_p(gU), _p(gS), _p(gV), _p(U), _p(S), _p(V), _p(gA), n)
+    return gA.reshape(n, 3, 3)
+
+
+def max_threads():
+    return int(load().oracle_max_threads())

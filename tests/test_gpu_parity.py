@@ -1,0 +1,221 @@
+"""GPU parity: the CUDA path (through the C ABI) against the FP64 CPU oracle.
+
+Inputs are rounded to float32 before they reach either side, so the comparison
+isolates arithmetic.  Bars: rod force profile within 1e-4 relative, parameter
+gradients within 1e-3 relative (relative to the largest entry), as stated for
+the path; states within 1e-4 relative.
+"""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import golden_util as gu
+import oracle
+from diffstir_gb300 import scene as S
+from diffstir_gb300.scene import Scene
+from diffstir_gb300.simulator import Simulator
+
+pytestmark = pytest.mark.gpu
+
+FORCE_RTOL = 1e-4
+GRAD_RTOL = 1e-3
+
+
+def f32(a):
+    return np.asarray(a, dtype=np.float32).astype(np.float64)
+
+
+def rounded(sc):
+    """Copy of a scene with every input rounded to float32."""
+    return Scene(sc.desc, f32(sc.liquid_x), f32(sc.rod_x), f32(sc.container_x), f32(sc.trajectory),
+                 f32(sc.params), dict(sc.info))
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return float(np.abs(a - b).max() / max(np.abs(b).max(), 1e-30))
+
+
+def gpu_force_and_grad(sc, T, wts, ckpt=50, options=None, want_state0=False):
+    sim = Simulator(sc, max_steps=T, options=options)
+    force = sim.forward(T, ckpt_every=ckpt, record=True)
+    out = sim.backward(torch.as_tensor(wts[None], dtype=torch.float32, device='cuda'), want_state0=want_state0)
+    torch.cuda.synchronize()
+    st = sim.status()
+    if want_state0:
+        dp, ds = out
+        return force[0].cpu().numpy(), dp[0].cpu().numpy(), {k: v.cpu().numpy() for k, v in ds.items()}, st
+    return force[0].cpu().numpy(), out[0].cpu().numpy(), None, st
+
+
+def oracle_force_and_grad(sc, T, wts, want_state0=False):
+    _, dp, ds, st = oracle.grad(sc.desc, sc.params, sc.trajectory, T, sc.x0(), wts, want_state0=want_state0)
+    force, _, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, sc.x0())
+    return force, dp, ds
+
+
+def fixture_scene(name, model):
+    d = gu.load(name)
+    desc = gu.desc_from_fixture(d, model)
+    return Scene(desc, d['liquid_particles'], d['operator_particles'], d['container_particles'],
+                 d['operator_trajectory'], d['m%d_params' % model]), d
+
+
+@pytest.mark.parametrize('model', [0, 1, 2])
+def test_reference_scene_golden(model):
+    """Reference scene (container, rod particles, k=20000) built by the
+    reference's own code: GPU vs the FP64 oracle and vs the reference's
+    compute_loss gradient."""
+    sc, d = fixture_scene('ref_f64_g32', model)
+    sc = rounded(sc)
+    T = sc.n_steps
+    force_o, _, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, sc.x0())
+    loss, dF = gu.reference_loss_and_dforce(force_o, d['m%d_target' % model], T)
+    force_g, dp_g, _, st = gpu_force_and_grad(sc, T, dF)
+    assert st == 0
+    _, dp_o, _ = oracle_force_and_grad(sc, T, dF)
+    assert rel(force_g, force_o) < FORCE_RTOL
+    assert rel(dp_g, dp_o) < GRAD_RTOL, (dp_g, dp_o)
+    # and against the reference's own (float64) gradient, whose trajectory was not rounded
+    assert rel(dp_g, d['m%d_grad_params' % model]) < 5e-2
+
+
+@pytest.mark.parametrize('model,params', [(S.MODEL_HB, (0.5, 0.3, 0.7, 0.0)),
+                                          (S.MODEL_CARREAU, (2.0, 0.1, 0.6, 0.8)),
+                                          (S.MODEL_CROSS, (1.5, 0.2, 0.5, 1.2))])
+@pytest.mark.parametrize('j_mode', [S.J_DET, S.J_SVD])
+def test_cylinder_scene_parity(model, params, j_mode):
+    T = 40
+    sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, params=params, model=model,
+                                         j_mode=j_mode, seed=1))
+    wts = np.random.default_rng(0).normal(size=(T, 3))
+    force_g, dp_g, ds_g, st = gpu_force_and_grad(sc, T, wts, ckpt=7, want_state0=True)
+    assert st == 0
+    force_o, dp_o, ds_o = oracle_force_and_grad(sc, T, wts, want_state0=True)
+    assert rel(force_g, force_o) < FORCE_RTOL
+    idx = [0, 1, 2] if model == S.MODEL_HB else [0, 1, 2, 3]
+    assert rel(dp_g[idx], dp_o[idx]) < GRAD_RTOL, (dp_g, dp_o)
+    assert rel(ds_g['x'], ds_o[:, 0:3]) < 1e-2
+    assert rel(ds_g['F'].reshape(-1, 9), ds_o[:, 15:24]) < 1e-2
+
+
+def test_forward_states_match_oracle():
+    T = 30
+    sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=4, n_steps=T, seed=2))
+    sim = Simulator(sc, max_steps=T)
+    sim.forward(T)
+    st = sim.get_state()
+    _, states, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, sc.x0(), return_states=True)
+    last = states[T]
+    assert rel(st['x'].cpu().numpy(), last[:, 0:3]) < 1e-5
+    assert rel(st['v'].cpu().numpy(), last[:, 3:6]) < 1e-3
+    assert rel(st['C'].cpu().numpy().reshape(-1, 9), last[:, 6:15]) < 1e-3
+    assert rel(st['F'].cpu().numpy().reshape(-1, 9), last[:, 15:24]) < 1e-4
+
+
+def test_checkpoint_interval_invariance():
+    T = 24
+    sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=4))
+    wts = np.random.default_rng(3).normal(size=(T, 3))
+    grads = [gpu_force_and_grad(sc, T, wts, ckpt=k)[1] for k in (1, 5, 24)]
+    for g in grads[1:]:
+        assert rel(g, grads[0]) < 1e-4
+
+
+def test_p2g_variants_agree():
+    T = 20
+    sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=5))
+    wts = np.random.default_rng(4).normal(size=(T, 3))
+    f0, g0, _, _ = gpu_force_and_grad(sc, T, wts, options={'p2g': 0})
+    f1, g1, _, _ = gpu_force_and_grad(sc, T, wts, options={'p2g': 1})
+    assert rel(f1, f0) < 1e-5
+    assert rel(g1, g0) < 1e-4
+
+
+def test_batched_equals_single():
+    """Scenes of uneven size and different parameters/models in one handle give
+    the per-scene results."""
+    T = 20
+    scenes = [rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=s, hi=(0.7, h, 0.7),
+                                              params=p, model=m))
+              for s, h, p, m in ((0, 0.30, (0.5, 0.0, 0.7, 0.0), S.MODEL_HB),
+                                 (1, 0.42, (2.0, 0.1, 0.6, 0.8), S.MODEL_CARREAU),
+                                 (2, 0.22, (0.9, 0.4, 0.8, 0.0), S.MODEL_HB))]
+    wts = np.random.default_rng(5).normal(size=(len(scenes), T, 3))
+    sim = Simulator(scenes, max_steps=T)
+    force = sim.forward(T, ckpt_every=6, record=True).cpu().numpy()
+    dp = sim.backward(torch.as_tensor(wts, dtype=torch.float32, device='cuda')).cpu().numpy()
+    for b, sc in enumerate(scenes):
+        f1, g1, _, _ = gpu_force_and_grad(sc, T, wts[b], ckpt=6)
+        assert rel(force[b], f1) < 1e-5
+        assert rel(dp[b], g1) < 1e-4
+
+
+def test_reference_scene_rod_particles_71():
+    path = os.path.join(gu.GOLDEN_DIR, 'ref_f64_g71.npz')
+    if not os.path.exists(path):
+        pytest.skip('fixture not generated')
+    sc, d = fixture_scene('ref_f64_g71', 2)
+    sc = rounded(sc)
+    T = sc.n_steps
+    force_o, _, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, sc.x0())
+    _, dF = gu.reference_loss_and_dforce(force_o, d['m2_target'], T)
+    force_g, dp_g, _, _ = gpu_force_and_grad(sc, T, dF)
+    _, dp_o, _ = oracle_force_and_grad(sc, T, dF)
+    assert rel(force_g, force_o) < FORCE_RTOL
+    assert rel(dp_g, dp_o) < GRAD_RTOL
+
+
+def test_autograd_function_matches_backward():
+    T = 16
+    sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=6))
+    sim = Simulator(sc, max_steps=T)
+    params = torch.tensor(sc.params[None], dtype=torch.float32, device='cuda', requires_grad=True)
+    target = torch.zeros((1, T, 3), device='cuda')
+    force = sim.rollout(params, ckpt_every=4)
+    loss = ((force[..., [0, 2]] - target[..., [0, 2]]) ** 2).mean()
+    loss.backward()
+    wts = (2 * force.detach() / (T * 2)).cpu().numpy()[0]
+    wts[:, 1] = 0
+    _, dp, _, _ = gpu_force_and_grad(sc, T, wts, ckpt=4)
+    assert rel(params.grad[0].cpu().numpy(), dp) < 1e-4
+
+
+def test_svd_kernels_match_oracle():
+    from diffstir_gb300 import ops
+    rng = np.random.default_rng(0)
+    A = rng.normal(size=(512, 3, 3)).astype(np.float32)
+    A[:128] = (np.eye(3) + 0.05 * rng.normal(size=(128, 3, 3))).astype(np.float32)
+    U, Sg, V = ops.svd3(torch.from_numpy(A).cuda())
+    U, Sg, V = U.cpu().numpy(), Sg.cpu().numpy(), V.cpu().numpy()
+    rec = np.einsum('nij,nj,nkj->nik', U, Sg, V)
+    np.testing.assert_allclose(rec, A, atol=2e-5 * np.abs(A).max())
+    assert np.all(np.linalg.det(U) > 0) and np.all(np.linalg.det(V) > 0)
+    np.testing.assert_allclose(np.abs(Sg), np.linalg.svd(A.astype(np.float64), compute_uv=False), rtol=1e-4,
+                               atol=1e-5)
+    gU, gS, gV = (rng.normal(size=(512, 3, 3)), rng.normal(size=(512, 3)), rng.normal(size=(512, 3, 3)))
+    Uo, So, Vo = oracle.svd3(A.astype(np.float64))
+    gA_o = oracle.svd3_backward(gU, gS, gV, Uo, So, Vo)
+    t = lambda a: torch.as_tensor(np.asarray(a, np.float32)).cuda()
+    gA = ops.svd3_backward(t(gU), t(gS), t(gV), t(Uo), t(So), t(Vo)).cpu().numpy()
+    err = np.abs(gA - gA_o).max(axis=(1, 2)) / np.maximum(np.abs(gA_o).max(axis=(1, 2)), 1.0)
+    assert np.median(err) < 1e-4 and np.max(err) < 1e-2
+
+
+def test_out_of_grid_particle_sets_status_and_is_skipped():
+    T = 4
+    sc = S.small_synthetic_scene(n_grid=16, ppc=1, n_steps=T, seed=0)
+    x = sc.x0()
+    x[0] = (-0.5, 0.5, 0.5)   # base < 0
+    x[1] = (2.0, 0.5, 0.5)    # base > n-3
+    sc.liquid_x = x
+    sim = Simulator(sc, max_steps=T)
+    sim.forward(T)
+    torch.cuda.synchronize()
+    flags = sim.status()
+    assert flags & 2
+    st = sim.get_state()
+    assert torch.isfinite(st['x'][2:]).all()

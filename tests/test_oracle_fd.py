@@ -1,0 +1,122 @@
+"""Central finite differences of the FP64 oracle (its adjoint is exact for the
+restated equations), on the parts of the path the reference scene does not
+exercise: the moving-cylinder rod, the SVD-determinant mode, the three models
+with the MSE force loss of the synthetic scenes, and the SVD kernels."""
+
+import numpy as np
+import pytest
+
+import oracle
+from diffstir_gb300 import scene as S
+
+
+def _loss_and_grad(sc, T, wts, params=None, want_state0=False, x0=None):
+    p = sc.params if params is None else params
+    x = sc.x0() if x0 is None else x0
+    force, _, _ = oracle.rollout(sc.desc, p, sc.trajectory, T, x)
+    loss = float((wts * force).sum())
+    _, dp, ds, _ = oracle.grad(sc.desc, p, sc.trajectory, T, x, wts, want_state0=want_state0)
+    return loss, dp, ds
+
+
+def _fd_params(sc, T, wts, idx, h_rel=1e-6):
+    out = []
+    for i in idx:
+        p = sc.params.copy()
+        h = h_rel * max(abs(p[i]), 1e-3)
+        p[i] += h
+        fp, _, _ = oracle.rollout(sc.desc, p, sc.trajectory, T, sc.x0())
+        p[i] -= 2 * h
+        fm, _, _ = oracle.rollout(sc.desc, p, sc.trajectory, T, sc.x0())
+        out.append(float((wts * (fp - fm)).sum()) / (2 * h))
+    return np.array(out)
+
+
+MODELS = [
+    (S.MODEL_HB, (0.5, 0.3, 0.7, 0.0), (0, 1, 2)),
+    (S.MODEL_CARREAU, (2.0, 0.1, 0.6, 0.8), (0, 1, 2, 3)),
+    (S.MODEL_CROSS, (1.5, 0.2, 0.5, 1.2), (0, 1, 2, 3)),
+]
+
+
+@pytest.mark.parametrize('model,params,idx', MODELS)
+@pytest.mark.parametrize('j_mode', [S.J_DET, S.J_SVD])
+def test_cylinder_scene_param_grad_fd(model, params, idx, j_mode):
+    T = 12
+    sc = S.small_synthetic_scene(n_grid=12, ppc=2, n_steps=T, params=params, model=model, j_mode=j_mode,
+                                 seed=3, dt=5e-4)
+    rng = np.random.default_rng(7)
+    wts = rng.normal(size=(T, 3))
+    loss, dp, _ = _loss_and_grad(sc, T, wts)
+    fd = _fd_params(sc, T, wts, idx)
+    assert np.any(np.abs(fd) > 0)
+    np.testing.assert_allclose(dp[list(idx)], fd, rtol=2e-5, atol=1e-9 * np.abs(fd).max())
+
+
+def test_cylinder_scene_state_grad_fd():
+    T = 10
+    sc = S.small_synthetic_scene(n_grid=12, ppc=2, n_steps=T, seed=5, dt=5e-4)
+    rng = np.random.default_rng(1)
+    wts = rng.normal(size=(T, 3))
+    _, _, ds = _loss_and_grad(sc, T, wts, want_state0=True)
+    x0 = sc.x0()
+    for p in rng.choice(x0.shape[0], 4, replace=False):
+        for c in range(3):
+            h = 1e-7
+            xp, xm = x0.copy(), x0.copy()
+            xp[p, c] += h
+            xm[p, c] -= h
+            fp, _, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, xp)
+            fm, _, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, xm)
+            fd = float((wts * (fp - fm)).sum()) / (2 * h)
+            assert abs(ds[p, c] - fd) <= 1e-4 * max(abs(fd), np.abs(ds[:, :3]).max() * 1e-2), (p, c, ds[p, c], fd)
+
+
+def test_reference_scene_param_grad_fd():
+    """Reference scene (container, rod particles, k=20000), L1 loss as compute_loss."""
+    T = 6
+    sc = S.reference_scene(seed=0, n_steps=T, n_liquid=300, n_rod=40, n_container=60, n_grid=32,
+                           model=S.MODEL_CARREAU, params=(2.0, 0.1, 0.6, 0.8))
+    rng = np.random.default_rng(2)
+    wts = rng.normal(size=(T, 3))
+    _, dp, _ = _loss_and_grad(sc, T, wts)
+    fd = _fd_params(sc, T, wts, (0, 1, 2, 3))
+    np.testing.assert_allclose(dp, fd, rtol=2e-4, atol=1e-6 * np.abs(fd).max())
+
+
+def test_svd3_matches_numpy():
+    rng = np.random.default_rng(0)
+    A = rng.normal(size=(200, 3, 3))
+    A[:50] = np.eye(3) + 0.05 * rng.normal(size=(50, 3, 3))
+    A[50:60] = np.diag([1.0, 1.0, 1.0]) + 1e-7 * rng.normal(size=(10, 3, 3))
+    U, Sg, V = oracle.svd3(A)
+    rec = np.einsum('nij,nj,nkj->nik', U, Sg, V)
+    np.testing.assert_allclose(rec, A, atol=1e-10)
+    eye = np.broadcast_to(np.eye(3), U.shape)
+    np.testing.assert_allclose(np.einsum('nji,njk->nik', U, U), eye, atol=1e-10)
+    np.testing.assert_allclose(np.einsum('nji,njk->nik', V, V), eye, atol=1e-10)
+    assert np.all(np.linalg.det(U) > 0) and np.all(np.linalg.det(V) > 0)
+    ref = np.linalg.svd(A, compute_uv=False)
+    np.testing.assert_allclose(np.abs(Sg), ref, rtol=1e-9, atol=1e-12)
+    assert np.all(Sg[:, 0] >= Sg[:, 1]) and np.all(Sg[:, 1] >= np.abs(Sg[:, 2]) - 1e-12)
+    np.testing.assert_allclose(np.sign(Sg[:, 2]), np.sign(np.linalg.det(A)))
+
+
+def test_svd3_backward_fd():
+    rng = np.random.default_rng(1)
+    A = rng.normal(size=(20, 3, 3))
+    gU, gS, gV = rng.normal(size=(20, 3, 3)), rng.normal(size=(20, 3)), rng.normal(size=(20, 3, 3))
+    U, Sg, V = oracle.svd3(A)
+    gA = oracle.svd3_backward(gU, gS, gV, U, Sg, V)
+    h = 1e-6
+    for n in range(5):
+        for i in range(3):
+            for j in range(3):
+                Ap, Am = A[n:n + 1].copy(), A[n:n + 1].copy()
+                Ap[0, i, j] += h
+                Am[0, i, j] -= h
+                Up, Sp, Vp = oracle.svd3(Ap)
+                Um, Sm, Vm = oracle.svd3(Am)
+                L = lambda u, s, v: (gU[n] * u[0]).sum() + (gS[n] * s[0]).sum() + (gV[n] * v[0]).sum()
+                fd = (L(Up, Sp, Vp) - L(Um, Sm, Vm)) / (2 * h)
+                assert abs(gA[n, i, j] - fd) < 1e-5 * max(1.0, abs(fd)), (n, i, j, gA[n, i, j], fd)
