@@ -46,7 +46,7 @@ KERNEL_BYTES = {
     'p2g': (132, 16), 'grid': (0, 44), 'g2p': (72, 12),
     'g2p_adj': (84, 24), 'grid_adj': (0, 56), 'p2g_adj': (240, 16),
 }
-KERNELS = ['p2g', 'grid', 'g2p', 'g2p_adj', 'grid_adj', 'p2g_adj', 'other']
+KERNELS = ['p2g', 'grid', 'g2p', 'g2p_adj', 'grid_adj', 'p2g_adj', 'bin', 'other']
 
 
 def parse():
@@ -58,7 +58,10 @@ def parse():
     ap.add_argument('--config', default='C2')
     ap.add_argument('--substeps', type=int, default=None, help='override the substep count')
     ap.add_argument('--ckpt', type=int, default=None)
-    ap.add_argument('--p2g', type=int, default=None)
+    ap.add_argument('--p2g', type=int, default=None, help='0 scalar atomics, 1 vector atomics, 2 binned cells')
+    ap.add_argument('--graph', type=int, default=None, help='1: replay rollouts as CUDA graphs')
+    ap.add_argument('--block', type=int, default=None)
+    ap.add_argument('--gblock', type=int, default=None)
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')
@@ -212,8 +215,9 @@ def run_ours(args):
 
     sc, T, ckpt = build_workload(args, rank)
     opts = {}
-    if args.p2g is not None:
-        opts['p2g'] = args.p2g
+    for k in ('p2g', 'graph', 'block', 'gblock'):
+        if getattr(args, k) is not None:
+            opts[k] = getattr(args, k)
     sim = Simulator(sc, max_steps=T, options=opts)
     dev = torch.device('cuda', local)
     N = sc.n_particles
@@ -359,6 +363,7 @@ def run_ours(args):
         'cpu_baseline': cpu,
         'e2e': e2e,
         'gpu_launches': int(launches),
+        'options': {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock')},
         'clocks': clk,
         'status_flags': int(st),
     }

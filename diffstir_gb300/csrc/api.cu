@@ -24,8 +24,8 @@ using namespace dstir;
 
 namespace {
 // kernel kinds timed by the optional in-library profiler
-enum { K_P2G = 0, K_GRID, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_OTHER, K_NUM };
-const char* const kKernelNames[K_NUM] = {"p2g", "grid", "g2p", "g2p_adj", "grid_adj", "p2g_adj", "other"};
+enum { K_P2G = 0, K_GRID, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_BIN, K_OTHER, K_NUM };
+const char* const kKernelNames[K_NUM] = {"p2g", "grid", "g2p", "g2p_adj", "grid_adj", "p2g_adj", "bin", "other"};
 
 // CUDA-event timing of every launch on the launching stream.  Event pairs live
 // in a ring; a pair is read back (synchronising on its stop event) when the
@@ -133,8 +133,31 @@ struct DstirHandle {
     unsigned* counters = nullptr;
     unsigned* status = nullptr;
 
+    // per-substep binning (p2g variant P2G_CELL); one (cell_start, perm) slot per
+    // substep of a segment, so the reverse pass reuses the recompute's bins
+    int* cnt = nullptr;         // [G+1]
+    int* bkey = nullptr;        // [stride]
+    int* brank = nullptr;       // [stride]
+    int* bsum = nullptr;        // scan scratch
+    int* cell_start = nullptr;  // [bin_slots][G+2]
+    int* perm = nullptr;        // [bin_slots][stride]
+    long long bin_slots = 0;
+    bool any_svd = false;
+
     Profiler prof;
     long long launches = 0;  // kernel launches issued since the counter was reset
+
+    // CUDA graphs: the whole forward rollout and the whole reverse pass are
+    // captured once per shape on a library-owned stream and replayed
+    float* fbuf = nullptr;     // [B][max_steps][3] forces of the last forward
+    float* dfbuf = nullptr;    // [B][max_steps][3] dL/dforce of the current backward
+    float* dpbuf = nullptr;    // [B][4] dL/dparams
+    long long epoch = 0;       // bumped on every (re)allocation; part of the graph keys
+    bool capturing = false;
+    cudaStream_t gstream = nullptr;
+    cudaEvent_t ev_in = nullptr, ev_out = nullptr;
+    cudaGraphExec_t fwd_exec = nullptr, bwd_exec = nullptr;
+    long long fwd_key[8] = {0}, bwd_key[8] = {0};
 
     int cur = 0;  // work slot holding the current state
     bool recorded = false;
@@ -163,6 +186,7 @@ int fail(DstirHandle* h, int code, const char* fmt, ...) {
 
 template <class T>
 int dalloc(DstirHandle* h, T** p, size_t count, const char* what) {
+    if (h) ++h->epoch;
     if (*p) cudaFree(*p);
     *p = nullptr;
     if (count == 0) count = 1;
@@ -270,7 +294,7 @@ FwdArgs fwd_args(DstirHandle* h, const float* cur, float* next, float4* pm, floa
 template <class Fn>
 void timed(DstirHandle* h, int kind, cudaStream_t st, Fn fn) {
     ++h->launches;
-    if (!h->prof.on) {
+    if (!h->prof.on || h->capturing) {
         fn();
         return;
     }
@@ -279,17 +303,66 @@ void timed(DstirHandle* h, int kind, cudaStream_t st, Fn fn) {
     h->prof.end(i, st);
 }
 
-void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st) {
-    timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, st); });
+int ensure_bin_slots(DstirHandle* h, long long n) {
+    if (n <= h->bin_slots) return DSTIR_OK;
+    int rc;
+    if (!h->cnt) {
+        if ((rc = dalloc(h, &h->cnt, (size_t)(h->G + 1), "bin counts"))) return rc;
+        CUDA_TRY(h, cudaMemset(h->cnt, 0, (size_t)(h->G + 1) * sizeof(int)));
+        if ((rc = dalloc(h, &h->bkey, (size_t)h->stride, "bin keys"))) return rc;
+        if ((rc = dalloc(h, &h->brank, (size_t)h->stride, "bin ranks"))) return rc;
+        if ((rc = dalloc(h, &h->bsum, (size_t)bin_scan_blocks(h->G), "scan scratch"))) return rc;
+    }
+    if ((rc = dalloc(h, &h->cell_start, (size_t)(n * (h->G + 2)), "cell starts"))) return rc;
+    if ((rc = dalloc(h, &h->perm, (size_t)(n * h->stride), "bin permutation"))) return rc;
+    h->bin_slots = n;
+    return DSTIR_OK;
+}
+
+int* slot_cell_start(DstirHandle* h, int slot) { return h->cell_start + (size_t)slot * (h->G + 2); }
+int* slot_perm(DstirHandle* h, int slot) { return h->perm + (size_t)slot * h->stride; }
+
+// One forward substep.  With the binned variant the particles of `a.cur` are
+// counting-sorted into bin slot `bin_slot` first.
+void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot = 0) {
+    if (h->p2g_variant == P2G_CELL) {
+        BinArgs b;
+        b.sc = h->sc;
+        b.blk = h->blk;
+        b.cur = a.cur;
+        b.stride = h->stride;
+        b.cnt = h->cnt;
+        b.key = h->bkey;
+        b.rank = h->brank;
+        b.cell_start = slot_cell_start(h, bin_slot);
+        b.perm = slot_perm(h, bin_slot);
+        b.bsum = h->bsum;
+        b.G = h->G;
+        b.status = h->status;
+        h->launches += 4;
+        timed(h, K_BIN, st, [&] { launch_bin(b, h->n_blocks, h->block, st); });
+        timed(h, K_P2G, st, [&] {
+            launch_p2g_cell(a, b.cell_start, b.perm, h->n_gblocks, h->gblock, h->G, h->any_svd, st);
+        });
+    } else {
+        timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st); });
+    }
     timed(h, K_GRID, st, [&] { launch_grid(a, h->n_gblocks, h->gblock, st); });
     timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st); });
 }
 
-void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st) {
-    int var = h->p2g_variant == P2G_PLAIN ? P2G_PLAIN : P2G_VEC;
-    timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st); });
+void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st, int bin_slot = 0) {
+    if (h->p2g_variant == P2G_CELL) {
+        timed(h, K_G2P_ADJ, st, [&] {
+            launch_g2p_adj_cell(a, slot_cell_start(h, bin_slot), slot_perm(h, bin_slot), h->n_gblocks, h->gblock,
+                                h->G, st);
+        });
+    } else {
+        int var = h->p2g_variant == P2G_PLAIN ? P2G_PLAIN : P2G_VEC;
+        timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st); });
+    }
     timed(h, K_GRID_ADJ, st, [&] { launch_grid_adj(a, h->n_gblocks, h->gblock, st); });
-    timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, st); });
+    timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st); });
 }
 
 }  // namespace
@@ -347,6 +420,7 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
         sd.cr2 = d.container_r * d.container_r;
         sd.rod_r2 = d.rod_radius * d.rod_radius;
         h->sc_h.push_back(sd);
+        if (d.j_mode == DSTIR_J_SVD) h->any_svd = true;
         p0 += (long long)d.n_liquid + d.n_rod + d.n_container;
         g0 += (long long)d.n_grid * d.n_grid * d.n_grid;
     }
@@ -365,6 +439,9 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
         (rc = dalloc(h, &h->params, (size_t)batch * 4, "parameters")) ||
         (rc = dalloc(h, &h->models, (size_t)batch, "models")) ||
         (rc = dalloc(h, &h->force_scratch, (size_t)batch * max_steps * 3, "force scratch")) ||
+        (rc = dalloc(h, &h->fbuf, (size_t)batch * max_steps * 3, "forces")) ||
+        (rc = dalloc(h, &h->dfbuf, (size_t)batch * max_steps * 3, "force adjoint")) ||
+        (rc = dalloc(h, &h->dpbuf, (size_t)batch * 4, "parameter adjoint")) ||
         (rc = dalloc(h, &h->pgrad, (size_t)max_steps * batch * 4, "parameter gradients")) ||
         (rc = dalloc(h, &h->counters, (size_t)3 * batch, "counters")) ||
         (rc = dalloc(h, &h->status, 1, "status")) || (rc = ensure_grid_slots(h, 1)) || (rc = build_tables(h))) {
@@ -392,8 +469,17 @@ void dstir_destroy(DstirHandle* h) {
     if (!h) return;
     h->prof.drain();
     h->prof.destroy();
+    if (h->fwd_exec) cudaGraphExecDestroy(h->fwd_exec);
+    if (h->bwd_exec) cudaGraphExecDestroy(h->bwd_exec);
+    if (h->gstream) {
+        cudaStreamSynchronize(h->gstream);
+        cudaStreamDestroy(h->gstream);
+    }
+    if (h->ev_in) cudaEventDestroy(h->ev_in);
+    if (h->ev_out) cudaEventDestroy(h->ev_out);
     void* ptrs[] = {h->sc, h->blk, h->gblk, h->work, h->ckpt, h->seg, h->pm, h->vo, h->ga, h->pmb, h->adj,
-                    h->traj, h->params, h->models, h->force_scratch, h->pgrad, h->partial, h->counters, h->status};
+                    h->traj, h->params, h->models, h->force_scratch, h->pgrad, h->partial, h->counters, h->status,
+                    h->cnt, h->bkey, h->brank, h->bsum, h->cell_start, h->perm, h->fbuf, h->dfbuf, h->dpbuf};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -445,6 +531,75 @@ int dstir_set_trajectory(DstirHandle* h, const float* traj, void* stream) {
     return DSTIR_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Enqueue a forward rollout; forces go to h->fbuf [B][max_steps][3] at fo = k.
+// Returns the work slot that holds the final state.
+int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, cudaStream_t st) {
+    size_t sf = slot_floats(h);
+    float* W[2] = {h->work, h->work + sf};
+    float* curp = W[h->cur];
+    if (record) cudaMemcpyAsync(h->ckpt, curp, sf * sizeof(float), cudaMemcpyDeviceToDevice, st);
+    cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st);
+    for (int k = 0; k < nsteps; ++k) {
+        bool boundary = record && ((k + 1) % K == 0) && (k + 1 < nsteps);
+        float* dst = boundary ? h->ckpt + (size_t)((k + 1) / K) * sf : (curp == W[0] ? W[1] : W[0]);
+        FwdArgs a = fwd_args(h, curp, dst, h->pm, h->vo, t0 + k, h->fbuf, (long long)h->max_steps * 3, k, 1);
+        run_substep(h, a, st);
+        curp = dst;
+    }
+    return (curp == W[0]) ? 0 : 1;
+}
+
+// Run `body(stream)` either directly on `st` or as a cached CUDA graph
+// replayed on the library stream (ordered after / before `st` by events).
+template <class Body>
+int run_maybe_graph(DstirHandle* h, cudaStream_t st, cudaGraphExec_t* exec, long long* key, const long long* want,
+                    Body body) {
+    if (!h->use_graph) {
+        body(st);
+        CUDA_TRY(h, cudaGetLastError());
+        return DSTIR_OK;
+    }
+    if (!h->gstream) {
+        CUDA_TRY(h, cudaStreamCreateWithFlags(&h->gstream, cudaStreamNonBlocking));
+        CUDA_TRY(h, cudaEventCreateWithFlags(&h->ev_in, cudaEventDisableTiming));
+        CUDA_TRY(h, cudaEventCreateWithFlags(&h->ev_out, cudaEventDisableTiming));
+    }
+    bool hit = *exec != nullptr;
+    for (int i = 0; i < 8 && hit; ++i) hit = key[i] == want[i];
+    if (!hit) {
+        if (*exec) cudaGraphExecDestroy(*exec);
+        *exec = nullptr;
+        cudaGraph_t g = nullptr;
+        CUDA_TRY(h, cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeThreadLocal));
+        h->capturing = true;
+        body(h->gstream);
+        h->capturing = false;
+        cudaError_t e = cudaStreamEndCapture(h->gstream, &g);
+        if (e != cudaSuccess) return fail(h, DSTIR_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            *exec = nullptr;
+            return fail(h, DSTIR_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+        }
+        for (int i = 0; i < 8; ++i) key[i] = want[i];
+    }
+    CUDA_TRY(h, cudaEventRecord(h->ev_in, st));
+    CUDA_TRY(h, cudaStreamWaitEvent(h->gstream, h->ev_in, 0));
+    CUDA_TRY(h, cudaGraphLaunch(*exec, h->gstream));
+    CUDA_TRY(h, cudaEventRecord(h->ev_out, h->gstream));
+    CUDA_TRY(h, cudaStreamWaitEvent(st, h->ev_out, 0));
+    return DSTIR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
 int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every, int32_t record, float* force_out,
                   void* stream) {
     if (!h) return DSTIR_EINVAL;
@@ -461,22 +616,28 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
         if ((rc = dalloc(h, &h->ckpt, (size_t)nseg * slot_floats(h), "checkpoints"))) return rc;
         h->ckpt_slots = nseg;
     }
-    float* force = force_out ? force_out : h->force_scratch;
-    long long fstride = force_out ? (long long)nsteps * 3 : (long long)h->max_steps * 3;
-    size_t sf = slot_floats(h);
-    float* W[2] = {h->work, h->work + sf};
-    float* curp = W[h->cur];
-    if (record) CUDA_TRY(h, cudaMemcpyAsync(h->ckpt, curp, sf * sizeof(float), cudaMemcpyDeviceToDevice, st));
-    CUDA_TRY(h, cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st));
-    for (int k = 0; k < nsteps; ++k) {
-        bool boundary = record && ((k + 1) % K == 0) && (k + 1 < nsteps);
-        float* dst = boundary ? h->ckpt + (size_t)((k + 1) / K) * sf : (curp == W[0] ? W[1] : W[0]);
-        FwdArgs a = fwd_args(h, curp, dst, h->pm, h->vo, t0 + k, force, fstride, k, 1);
-        run_substep(h, a, st);
-        curp = dst;
+    if (h->p2g_variant == P2G_CELL && (rc = ensure_bin_slots(h, 1))) return rc;
+    long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch, h->p2g_variant, h->block * 4096 + h->gblock};
+    int final_slot = 0;
+    rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want,
+                         [&](cudaStream_t s2) { final_slot = enqueue_forward(h, t0, nsteps, K, record != 0, s2); });
+    if (rc) return rc;
+    if (h->use_graph) {
+        // the slot sequence is fixed by (cur, nsteps, K, record): replay it on the host
+        size_t sf = slot_floats(h);
+        float* W[2] = {h->work, h->work + sf};
+        float* curp = W[h->cur];
+        for (int k = 0; k < nsteps; ++k) {
+            bool boundary = record && ((k + 1) % K == 0) && (k + 1 < nsteps);
+            curp = boundary ? h->ckpt + (size_t)((k + 1) / K) * sf : (curp == W[0] ? W[1] : W[0]);
+        }
+        final_slot = (curp == W[0]) ? 0 : 1;
     }
-    CUDA_TRY(h, cudaGetLastError());
-    h->cur = (curp == W[0]) ? 0 : 1;
+    h->cur = final_slot;
+    if (force_out)
+        CUDA_TRY(h, cudaMemcpy2DAsync(force_out, (size_t)nsteps * 3 * sizeof(float), h->fbuf,
+                                      (size_t)h->max_steps * 3 * sizeof(float), (size_t)nsteps * 3 * sizeof(float),
+                                      (size_t)h->B, cudaMemcpyDeviceToDevice, st));
     if (record) {
         h->recorded = true;
         h->rec_t0 = t0;
@@ -491,6 +652,8 @@ int dstir_substep(DstirHandle* h, int32_t f, float* force_out, void* stream) {
     if (f < 0 || f >= h->max_steps) return fail(h, DSTIR_EINVAL, "dstir_substep: f=%d outside [0,%d)", f, h->max_steps);
     cudaStream_t st = S(stream);
     h->recorded = false;
+    int rc;
+    if (h->p2g_variant == P2G_CELL && (rc = ensure_bin_slots(h, 1))) return rc;
     size_t sf = slot_floats(h);
     float* W[2] = {h->work, h->work + sf};
     float* force = force_out ? force_out : h->force_scratch;
@@ -503,37 +666,32 @@ int dstir_substep(DstirHandle* h, int32_t f, float* force_out, void* stream) {
     return DSTIR_OK;
 }
 
-int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, float* dL_dx0, float* dL_dv0,
-                   float* dL_dC0, float* dL_dF0, void* stream) {
-    if (!h) return DSTIR_EINVAL;
-    if (!h->recorded) return fail(h, DSTIR_ESTATE, "dstir_backward: no recorded forward (record=1) to differentiate");
-    if (!dL_dforce) return fail(h, DSTIR_EINVAL, "dstir_backward: dL_dforce is required");
-    cudaStream_t st = S(stream);
+}  // extern "C"
+
+namespace {
+
+// Enqueue the reverse pass of the recorded rollout.  dL/dforce is read from
+// h->dfbuf ([B][max_steps][3], entry fo = substep - t0); dL/dparams goes to
+// h->dpbuf.  Returns the adjoint slot holding dL/d(step-0 state).
+int enqueue_backward(DstirHandle* h, cudaStream_t st) {
     const int n = h->rec_n, K = h->rec_K, t0 = h->rec_t0;
     const long long nseg = (n + K - 1) / K;
     size_t sf = slot_floats(h);
-    int rc;
-    if (K > h->seg_slots) {
-        if ((rc = dalloc(h, &h->seg, (size_t)K * sf, "segment states"))) return rc;
-        h->seg_slots = K;
-    }
-    if ((rc = ensure_grid_slots(h, K))) return rc;
     float* A[2] = {h->adj, h->adj + sf};
     int nx = 0;
-    CUDA_TRY(h, cudaMemsetAsync(A[nx], 0, sf * sizeof(float), st));
-    CUDA_TRY(h, cudaMemsetAsync(h->ga, 0, (size_t)h->G * sizeof(float4), st));
-    CUDA_TRY(h, cudaMemsetAsync(h->pgrad, 0, (size_t)n * h->B * 4 * sizeof(float), st));
-    const long long fstride = (long long)n * 3;
+    cudaMemsetAsync(A[nx], 0, sf * sizeof(float), st);
+    cudaMemsetAsync(h->ga, 0, (size_t)h->G * sizeof(float4), st);
+    cudaMemsetAsync(h->pgrad, 0, (size_t)n * h->B * 4 * sizeof(float), st);
     for (long long sgi = nseg - 1; sgi >= 0; --sgi) {
         int s0 = (int)(sgi * K);
         int L = std::min(K, n - s0);
         float* slot0 = h->ckpt + (size_t)sgi * sf;
         auto slot = [&](int j) -> float* { return j == 0 ? slot0 : h->seg + (size_t)(j - 1) * sf; };
-        CUDA_TRY(h, cudaMemsetAsync(h->pm, 0, (size_t)L * h->G * sizeof(float4), st));
+        cudaMemsetAsync(h->pm, 0, (size_t)L * h->G * sizeof(float4), st);
         for (int k = 0; k < L; ++k) {
             FwdArgs a = fwd_args(h, slot(k), slot(k + 1), h->pm + (size_t)k * h->G, h->vo + (size_t)k * h->G,
                                  t0 + s0 + k, h->force_scratch, (long long)h->max_steps * 3, t0 + s0 + k, 0);
-            run_substep(h, a, st);
+            run_substep(h, a, st, k);
         }
         for (int k = L - 1; k >= 0; --k) {
             AdjArgs a;
@@ -553,23 +711,56 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
             a.f = t0 + s0 + k;
             a.params = h->params;
             a.models = h->models;
-            a.dforce = dL_dforce;
-            a.dforce_stride = fstride;
+            a.dforce = h->dfbuf;
+            a.dforce_stride = (long long)h->max_steps * 3;
             a.fo = s0 + k;
             a.pgrad = h->pgrad;
             a.partial = h->partial;
             a.counters = h->counters;
             a.batch = h->B;
-            run_adj_substep(h, a, st);
+            run_adj_substep(h, a, st, k);
             nx = 1 - nx;
         }
     }
-    CUDA_TRY(h, cudaGetLastError());
-    CUDA_TRY(h, cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st));
-    if (dL_dparams) timed(h, K_OTHER, st, [&] { launch_reduce_pgrad(h->pgrad, n, h->B, dL_dparams, st); });
+    cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st);
+    timed(h, K_OTHER, st, [&] { launch_reduce_pgrad(h->pgrad, n, h->B, h->dpbuf, st); });
+    return nx;
+}
+
+}  // namespace
+
+extern "C" {
+
+int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, float* dL_dx0, float* dL_dv0,
+                   float* dL_dC0, float* dL_dF0, void* stream) {
+    if (!h) return DSTIR_EINVAL;
+    if (!h->recorded) return fail(h, DSTIR_ESTATE, "dstir_backward: no recorded forward (record=1) to differentiate");
+    if (!dL_dforce) return fail(h, DSTIR_EINVAL, "dstir_backward: dL_dforce is required");
+    cudaStream_t st = S(stream);
+    const int n = h->rec_n, K = h->rec_K;
+    size_t sf = slot_floats(h);
+    int rc;
+    if (K > h->seg_slots) {
+        if ((rc = dalloc(h, &h->seg, (size_t)K * sf, "segment states"))) return rc;
+        h->seg_slots = K;
+    }
+    if ((rc = ensure_grid_slots(h, K))) return rc;
+    if (h->p2g_variant == P2G_CELL && (rc = ensure_bin_slots(h, K))) return rc;
+    // dL/dforce [B][n][3] -> internal [B][max_steps][3]
+    CUDA_TRY(h, cudaMemcpy2DAsync(h->dfbuf, (size_t)h->max_steps * 3 * sizeof(float), dL_dforce,
+                                  (size_t)n * 3 * sizeof(float), (size_t)n * 3 * sizeof(float), (size_t)h->B,
+                                  cudaMemcpyDeviceToDevice, st));
+    long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant, h->block * 4096 + h->gblock, 0, 0};
+    int final_nx = n % 2;
+    rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, [&](cudaStream_t s2) { enqueue_backward(h, s2); });
+    if (rc) return rc;
+    float* A[2] = {h->adj, h->adj + sf};
+    if (dL_dparams)
+        CUDA_TRY(h, cudaMemcpyAsync(dL_dparams, h->dpbuf, (size_t)h->B * 4 * sizeof(float), cudaMemcpyDeviceToDevice,
+                                    st));
     if (dL_dx0 || dL_dv0 || dL_dC0 || dL_dF0)
         timed(h, K_OTHER, st,
-              [&] { launch_unpack_state(A[nx], h->stride, h->N, dL_dx0, dL_dv0, dL_dC0, dL_dF0, st); });
+              [&] { launch_unpack_state(A[final_nx], h->stride, h->N, dL_dx0, dL_dv0, dL_dC0, dL_dF0, st); });
     CUDA_TRY(h, cudaGetLastError());
     return DSTIR_OK;
 }
@@ -589,6 +780,7 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     if (!strcmp(key, "p2g")) {
         if (value < 0 || value > 2) return fail(h, DSTIR_EINVAL, "p2g variant %lld not in 0..2", (long long)value);
         h->p2g_variant = (int)value;
+        h->recorded = false;
         return DSTIR_OK;
     }
     if (!strcmp(key, "block") || !strcmp(key, "gblock")) {

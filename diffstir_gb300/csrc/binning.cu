@@ -1,0 +1,455 @@
+// Per-substep particle binning by cell, and the binned scatter kernels.
+//
+// The reference scatters every particle to its 27 stencil nodes with one
+// global atomic per node and component (p2g, simulation_functions.py:155-163;
+// Taichi's g2p.grad does the transposed scatter).  Here the particles of each
+// substep are first counting-sorted by the cell of their stencil base
+// (bin_count -> 3-phase scan -> bin_scatter).  All particles of a cell share
+// the same 27 target nodes, so the binned kernels run one thread per cell: the
+// thread accumulates its particles' contributions in registers and issues one
+// vector atomic per node, i.e. 27 per occupied cell instead of 27 per
+// particle, and within a warp (32 neighbouring cells) no two lanes target the
+// same node in the same instruction.
+//
+// Particles whose stencil leaves the grid go to an overflow bin (index G) that
+// the extra last block of each binned kernel handles without scattering.
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "device_util.cuh"
+#include "internal.h"
+
+namespace dstir {
+
+constexpr int SCAN_THREADS = 256;
+constexpr int SCAN_PER_THREAD = 16;
+constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_PER_THREAD;
+
+// ---------------------------------------------------------------------------
+// counting sort by cell
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(256) bin_count_kernel(BinArgs b) {
+    __shared__ SceneDev s;
+    __shared__ BlockInfo bi;
+    if (threadIdx.x == 0) {
+        bi = b.blk[blockIdx.x];
+        s = b.sc[bi.scene];
+    }
+    __syncthreads();
+    long long p = bi.start + threadIdx.x;
+    bool active = p < bi.end;
+    long long key = -1;
+    if (active) {
+        float x[3];
+        load3(b.cur, b.stride, OX, p, x);
+        int base[3];
+        float fx[3];
+        if (locate(x, s.inv_dx, s.n, base, fx)) {
+            key = node_index(s, base[0], base[1], base[2]);
+        } else {
+            key = b.G;  // overflow bin
+            atomicOr(b.status, DSTIR_STATUS_OUT_OF_GRID);
+        }
+    }
+    // warp-aggregated increment: lanes with the same key share one atomic
+    const int lane = threadIdx.x & 31;
+    unsigned peers = __match_any_sync(0xffffffffu, key);
+    int leader = __ffs(peers) - 1;
+    int base_rank = 0;
+    if (key >= 0 && lane == leader) base_rank = atomicAdd(b.cnt + key, __popc(peers));
+    base_rank = __shfl_sync(0xffffffffu, base_rank, leader);
+    if (active) {
+        b.key[p] = (int)key;
+        b.rank[p] = base_rank + __popc(peers & ((1u << lane) - 1u));
+    }
+}
+
+// block sums of cnt[0, n) in chunks of SCAN_CHUNK
+__global__ void __launch_bounds__(SCAN_THREADS) scan_reduce_kernel(const int* cnt, long long n, int* bsum) {
+    __shared__ int sh[SCAN_THREADS / 32];
+    long long base = (long long)blockIdx.x * SCAN_CHUNK;
+    int acc = 0;
+    for (int i = threadIdx.x; i < SCAN_CHUNK; i += SCAN_THREADS) {
+        long long q = base + i;
+        if (q < n) acc += cnt[q];
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+    if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int t = 0;
+        for (int w = 0; w < SCAN_THREADS / 32; ++w) t += sh[w];
+        bsum[blockIdx.x] = t;
+    }
+}
+
+// exclusive scan of bsum[0, nb) in place (one block of 1024 threads)
+__global__ void __launch_bounds__(1024) scan_top_kernel(int* bsum, int nb) {
+    __shared__ int warp_tot[32];
+    const int per = (nb + 1023) / 1024;
+    const int t = threadIdx.x;
+    int local = 0;
+    for (int i = 0; i < per; ++i) {
+        int q = t * per + i;
+        if (q < nb) local += bsum[q];
+    }
+    // inclusive warp scan of the per-thread totals
+    int lane = t & 31, w = t >> 5;
+    int v = local;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        int u = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += u;
+    }
+    if (lane == 31) warp_tot[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int x = warp_tot[lane];
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += u;
+        }
+        warp_tot[lane] = x;
+    }
+    __syncthreads();
+    int excl = v - local + (w > 0 ? warp_tot[w - 1] : 0);
+    for (int i = 0; i < per; ++i) {
+        int q = t * per + i;
+        if (q < nb) {
+            int c = bsum[q];
+            bsum[q] = excl;
+            excl += c;
+        }
+    }
+}
+
+// cell_start[q] = exclusive prefix of cnt; cnt is zeroed for the next substep;
+// cell_start[n] = total
+__global__ void __launch_bounds__(SCAN_THREADS) scan_apply_kernel(int* cnt, long long n, const int* bsum,
+                                                                  int* cell_start) {
+    __shared__ int warp_tot[SCAN_THREADS / 32];
+    long long base = (long long)blockIdx.x * SCAN_CHUNK + (long long)threadIdx.x * SCAN_PER_THREAD;
+    int vals[SCAN_PER_THREAD];
+    int local = 0;
+#pragma unroll
+    for (int i = 0; i < SCAN_PER_THREAD; ++i) {
+        long long q = base + i;
+        vals[i] = (q < n) ? cnt[q] : 0;
+        local += vals[i];
+    }
+    int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int v = local;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        int u = __shfl_up_sync(0xffffffffu, v, off);
+        if (lane >= off) v += u;
+    }
+    if (lane == 31) warp_tot[w] = v;
+    __syncthreads();
+    if (w == 0) {
+        int x = lane < SCAN_THREADS / 32 ? warp_tot[lane] : 0;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            int u = __shfl_up_sync(0xffffffffu, x, off);
+            if (lane >= off) x += u;
+        }
+        if (lane < SCAN_THREADS / 32) warp_tot[lane] = x;
+    }
+    __syncthreads();
+    int excl = bsum[blockIdx.x] + v - local + (w > 0 ? warp_tot[w - 1] : 0);
+#pragma unroll
+    for (int i = 0; i < SCAN_PER_THREAD; ++i) {
+        long long q = base + i;
+        if (q < n) {
+            cell_start[q] = excl;
+            cnt[q] = 0;
+            excl += vals[i];
+            if (q == n - 1) cell_start[n] = excl;
+        }
+    }
+}
+
+__global__ void __launch_bounds__(256) bin_scatter_kernel(BinArgs b) {
+    __shared__ BlockInfo bi;
+    if (threadIdx.x == 0) bi = b.blk[blockIdx.x];
+    __syncthreads();
+    long long p = bi.start + threadIdx.x;
+    if (p >= bi.end) return;
+    int key = b.key[p];
+    b.perm[b.cell_start[key] + b.rank[p]] = (int)p;
+}
+
+void launch_bin(const BinArgs& b, int n_blocks, int block, cudaStream_t st) {
+    if (n_blocks <= 0) return;
+    long long n = b.G + 1;  // cells plus the overflow bin
+    int nb = (int)((n + SCAN_CHUNK - 1) / SCAN_CHUNK);
+    bin_count_kernel<<<n_blocks, block, 0, st>>>(b);
+    scan_reduce_kernel<<<nb, SCAN_THREADS, 0, st>>>(b.cnt, n, b.bsum);
+    scan_top_kernel<<<1, 1024, 0, st>>>(b.bsum, nb);
+    scan_apply_kernel<<<nb, SCAN_THREADS, 0, st>>>(b.cnt, n, b.bsum, b.cell_start);
+    bin_scatter_kernel<<<n_blocks, block, 0, st>>>(b);
+}
+
+int bin_scan_blocks(long long G) { return (int)((G + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK); }
+
+// ---------------------------------------------------------------------------
+// binned P2G: one thread per cell
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ int particle_kind(const SceneDev& s, long long p) {
+    long long q = p - s.p0;
+    return q < s.n_liquid ? KIND_LIQUID : (q < (long long)s.n_liquid + s.n_rod ? KIND_ROD : KIND_CONTAINER);
+}
+
+// Per-particle P2G quantities (p2g :111-153); writes F[f+1].
+template <bool SVDJ>
+__device__ __forceinline__ void p2g_particle(const FwdArgs& a, const SceneDev& s, const float* prm, int model,
+                                             long long p, int kind, float x[3], float& m, float mv[3], float A[9]) {
+    float v[3], C[9], F[9];
+    load3(a.cur, a.stride, OX, p, x);
+    load3(a.cur, a.stride, OV, p, v);
+    load9(a.cur, a.stride, OC, p, C);
+    load9(a.cur, a.stride, OF, p, F);
+    if (kind == KIND_LIQUID) {
+        LiquidP2G q;
+        liquid_p2g<SVDJ>(s, model, prm, v, C, F, q);
+        store9(a.next, a.stride, OF, p, q.Ft);
+        m = s.m_liq;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = q.A[i];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) mv[c] = m * q.vv[c];
+    } else {
+        store9(a.next, a.stride, OF, p, F);
+        m = (kind == KIND_ROD) ? s.m_rod : s.m_cont;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = m * C[i];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) mv[c] = m * v[c];
+    }
+}
+
+template <bool SVDJ>
+__global__ void __launch_bounds__(256) p2g_cell_kernel(FwdArgs a, const int* __restrict__ cell_start,
+                                                       const int* __restrict__ perm, int n_gblocks, long long G) {
+    __shared__ SceneDev s;
+    __shared__ GridBlock gb;
+    __shared__ float prm[4];
+    __shared__ int model;
+    const bool overflow = blockIdx.x == (unsigned)n_gblocks;
+    if (threadIdx.x == 0) {
+        gb = a.gblk[overflow ? 0 : blockIdx.x];
+        s = a.sc[gb.scene];
+    }
+    __syncthreads();
+    if (overflow) {
+        // particles outside the grid: F[f+1] only, no scatter (status was raised when binning)
+        int beg = cell_start[G], end = cell_start[G + 1];
+        for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+            long long p = perm[q];
+            int sc_i = 0;
+            while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
+            SceneDev s2 = a.sc[sc_i];
+            float pr[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) pr[i] = a.params[sc_i * 4 + i];
+            float x[3], m, mv[3], A[9];
+            p2g_particle<SVDJ>(a, s2, pr, a.models[sc_i], p, particle_kind(s2, p), x, m, mv, A);
+        }
+        return;
+    }
+    if (threadIdx.x < 4) prm[threadIdx.x] = a.params[gb.scene * 4 + threadIdx.x];
+    if (threadIdx.x == 0) model = a.models[gb.scene];
+    __syncthreads();
+    long long cell = gb.start + threadIdx.x;
+    if (cell >= gb.end) return;
+    int beg = cell_start[cell], end = cell_start[cell + 1];
+    if (beg == end) return;
+    long long local = cell - s.goff;
+    int n = s.n;
+    int bi = (int)(local / ((long long)n * n)), bj = (int)((local / n) % n), bk = (int)(local % n);
+    float acc[27][4];
+#pragma unroll
+    for (int o = 0; o < 27; ++o) acc[o][0] = acc[o][1] = acc[o][2] = acc[o][3] = 0.f;
+    for (int q = beg; q < end; ++q) {
+        long long p = perm[q];
+        float x[3], m, mv[3], A[9];
+        p2g_particle<SVDJ>(a, s, prm, model, p, particle_kind(s, p), x, m, mv, A);
+        float fx[3] = {x[0] * s.inv_dx - (float)bi, x[1] * s.inv_dx - (float)bj, x[2] * s.inv_dx - (float)bk};
+        float w[3][3];
+        bspline(fx, w);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                float wij = w[i][0] * w[j][1];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int o = (i * 3 + j) * 3 + k;
+                    float W = wij * w[k][2];
+                    float dp0 = ((float)i - fx[0]) * s.dx, dp1 = ((float)j - fx[1]) * s.dx,
+                          dp2 = ((float)k - fx[2]) * s.dx;
+                    acc[o][0] += W * (mv[0] + (A[0] * dp0 + A[1] * dp1 + A[2] * dp2));
+                    acc[o][1] += W * (mv[1] + (A[3] * dp0 + A[4] * dp1 + A[5] * dp2));
+                    acc[o][2] += W * (mv[2] + (A[6] * dp0 + A[7] * dp1 + A[8] * dp2));
+                    acc[o][3] += W * m;
+                }
+            }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            long long row = node_index(s, bi + i, bj + j, bk);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int o = (i * 3 + j) * 3 + k;
+                red_add4(a.pm + row + k, acc[o][0], acc[o][1], acc[o][2], acc[o][3]);
+            }
+        }
+}
+
+// ---------------------------------------------------------------------------
+// binned G2P adjoint (G2P^T): one thread per cell scatters into the grid
+// adjoint; the per-particle position adjoint is written as in g2p_adj_kernel
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void g2p_adj_particle_inputs(const AdjArgs& a, const SceneDev& s, const float* fb,
+                                                        long long p, int kind, float vnb[3], float xb[3],
+                                                        float Cb[9]) {
+    load9(a.adj_next, a.stride, OC, p, Cb);
+    if (kind == KIND_LIQUID) {
+        float ax[3], av[3];
+        load3(a.adj_next, a.stride, OX, p, ax);
+        load3(a.adj_next, a.stride, OV, p, av);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            vnb[c] = av[c] + s.dt * ax[c];
+            xb[c] = ax[c];
+        }
+    } else if (kind == KIND_ROD && s.rod_mode == DSTIR_ROD_PARTICLES) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            vnb[c] = -fb[c] * s.force_scale;
+            xb[c] = 0.f;
+        }
+    } else {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vnb[c] = xb[c] = 0.f;
+    }
+}
+
+__global__ void __launch_bounds__(256) g2p_adj_cell_kernel(AdjArgs a, const int* __restrict__ cell_start,
+                                                           const int* __restrict__ perm, int n_gblocks,
+                                                           long long G) {
+    __shared__ SceneDev s;
+    __shared__ GridBlock gb;
+    __shared__ float fb[3];
+    const bool overflow = blockIdx.x == (unsigned)n_gblocks;
+    if (overflow) {
+        // particles outside the grid: only x[f+1] = x[f] + dt v[f+1] carries an adjoint
+        int beg = cell_start[G], end = cell_start[G + 1];
+        for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+            long long p = perm[q];
+            int sc_i = 0;
+            while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
+            if (particle_kind(a.sc[sc_i], p) == KIND_LIQUID) {
+                float ax[3];
+                load3(a.adj_next, a.stride, OX, p, ax);
+                store3(a.adj_cur, a.stride, OX, p, ax);
+            }
+        }
+        return;
+    }
+    if (threadIdx.x == 0) {
+        gb = a.gblk[blockIdx.x];
+        s = a.sc[gb.scene];
+        const float* d = a.dforce + gb.scene * a.dforce_stride + (long long)a.fo * 3;
+        for (int c = 0; c < 3; ++c) fb[c] = d[c];
+    }
+    __syncthreads();
+    long long cell = gb.start + threadIdx.x;
+    if (cell >= gb.end) return;
+    int beg = cell_start[cell], end = cell_start[cell + 1];
+    if (beg == end) return;
+    long long local = cell - s.goff;
+    int n = s.n;
+    int bi = (int)(local / ((long long)n * n)), bj = (int)((local / n) % n), bk = (int)(local % n);
+    const float c4 = 4.f * s.inv_dx;
+    float acc[27][3];
+#pragma unroll
+    for (int o = 0; o < 27; ++o) acc[o][0] = acc[o][1] = acc[o][2] = 0.f;
+    for (int q = beg; q < end; ++q) {
+        long long p = perm[q];
+        int kind = particle_kind(s, p);
+        float x[3], vnb[3], xb[3], Cb[9];
+        load3(a.cur, a.stride, OX, p, x);
+        g2p_adj_particle_inputs(a, s, fb, p, kind, vnb, xb, Cb);
+        float fx[3] = {x[0] * s.inv_dx - (float)bi, x[1] * s.inv_dx - (float)bj, x[2] * s.inv_dx - (float)bk};
+        float w[3][3], dw[3][3];
+        bspline_d(fx, w, dw);
+        float fxb[3] = {0.f, 0.f, 0.f};
+        const bool liquid = kind == KIND_LIQUID;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j) {
+                long long row = node_index(s, bi + i, bj + j, bk);
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int o = (i * 3 + j) * 3 + k;
+                    float W = w[i][0] * w[j][1] * w[k][2];
+                    float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
+                    float Cd0 = Cb[0] * d0 + Cb[1] * d1 + Cb[2] * d2;
+                    float Cd1 = Cb[3] * d0 + Cb[4] * d1 + Cb[5] * d2;
+                    float Cd2 = Cb[6] * d0 + Cb[7] * d1 + Cb[8] * d2;
+                    acc[o][0] += W * (vnb[0] + c4 * Cd0);
+                    acc[o][1] += W * (vnb[1] + c4 * Cd1);
+                    acc[o][2] += W * (vnb[2] + c4 * Cd2);
+                    if (liquid) {
+                        float4 g = __ldg(a.vo + row + k);
+                        float Wb = vnb[0] * g.x + vnb[1] * g.y + vnb[2] * g.z +
+                                   c4 * (g.x * Cd0 + g.y * Cd1 + g.z * Cd2);
+                        fxb[0] -= c4 * W * (Cb[0] * g.x + Cb[3] * g.y + Cb[6] * g.z);
+                        fxb[1] -= c4 * W * (Cb[1] * g.x + Cb[4] * g.y + Cb[7] * g.z);
+                        fxb[2] -= c4 * W * (Cb[2] * g.x + Cb[5] * g.y + Cb[8] * g.z);
+                        fxb[0] += Wb * dw[i][0] * w[j][1] * w[k][2];
+                        fxb[1] += Wb * w[i][0] * dw[j][1] * w[k][2];
+                        fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
+                    }
+                }
+            }
+        if (liquid) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
+            store3(a.adj_cur, a.stride, OX, p, xb);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            long long row = node_index(s, bi + i, bj + j, bk);
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const int o = (i * 3 + j) * 3 + k;
+                red_add4(a.ga + row + k, acc[o][0], acc[o][1], acc[o][2], 0.f);
+            }
+        }
+}
+
+void launch_p2g_cell(const FwdArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
+                     long long G, bool svdj, cudaStream_t st) {
+    if (n_gblocks <= 0) return;
+    if (svdj)
+        p2g_cell_kernel<true><<<n_gblocks + 1, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
+    else
+        p2g_cell_kernel<false><<<n_gblocks + 1, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
+}
+
+void launch_g2p_adj_cell(const AdjArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
+                         long long G, cudaStream_t st) {
+    if (n_gblocks > 0) g2p_adj_cell_kernel<<<n_gblocks + 1, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
+}
+
+}  // namespace dstir

@@ -58,16 +58,40 @@ struct AdjArgs {
     int batch;
 };
 
-// p2g variants
-enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_TILE = 2 };
+// Counting sort of the particles of one substep by stencil-base cell.
+struct BinArgs {
+    const SceneDev* sc;
+    const BlockInfo* blk;
+    const float* cur;        // state whose positions are binned
+    long long stride;
+    int* cnt;                // [G+1] particles per cell (+ overflow bin G); zero on entry, zeroed on exit
+    int* key;                // [N] bin of each particle
+    int* rank;               // [N] position inside its bin
+    int* cell_start;         // [G+2] exclusive prefix of the counts
+    int* perm;               // [N] particle indices sorted by bin
+    int* bsum;               // scan scratch, bin_scan_blocks(G) entries
+    long long G;
+    unsigned* status;
+};
 
-void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, cudaStream_t st);
+// p2g variants: scalar atomics per particle, vector atomics per particle,
+// binned one-thread-per-cell accumulation
+enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_CELL = 2 };
+
+void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st);
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st);
 void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st);
 
 void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st);
 void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st);
-void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, cudaStream_t st);
+void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st);
+
+void launch_bin(const BinArgs& b, int n_blocks, int block, cudaStream_t st);
+int bin_scan_blocks(long long G);
+void launch_p2g_cell(const FwdArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
+                     long long G, bool svdj, cudaStream_t st);
+void launch_g2p_adj_cell(const AdjArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
+                         long long G, cudaStream_t st);
 
 void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
                        long long stride, long long n, cudaStream_t s);

@@ -17,136 +17,14 @@
 #include "common.cuh"
 #include "internal.h"
 #include "svd.cuh"
+#include "device_util.cuh"
 
 namespace dstir {
 
 // ---------------------------------------------------------------------------
-// reductions
-// ---------------------------------------------------------------------------
-template <int NV>
-__device__ __forceinline__ void block_reduce(float (&v)[NV], float (*sh)[4]) {
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-        for (int c = 0; c < NV; ++c) v[c] += __shfl_down_sync(0xffffffffu, v[c], off);
-    int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    __syncthreads();
-    if (lane == 0)
-#pragma unroll
-        for (int c = 0; c < NV; ++c) sh[warp][c] = v[c];
-    __syncthreads();
-    if (warp == 0) {
-        int nw = blockDim.x >> 5;
-#pragma unroll
-        for (int c = 0; c < NV; ++c) v[c] = lane < nw ? sh[lane][c] : 0.f;
-#pragma unroll
-        for (int off = 16; off > 0; off >>= 1)
-#pragma unroll
-            for (int c = 0; c < NV; ++c) v[c] += __shfl_down_sync(0xffffffffu, v[c], off);
-    }
-}
-
-// Every block of a (scene, purpose) group publishes its partial sum; the block
-// that arrives last adds the partials of the group in block order (so the
-// result does not depend on scheduling) and writes it to out[0..NV).
-template <int NV>
-__device__ __forceinline__ void group_sum(float (&v)[NV], float (*sh)[4], float* partial, unsigned* counter,
-                                          int group_first, int group_count, float* out, float scale) {
-    __shared__ bool is_last;
-    block_reduce<NV>(v, sh);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int c = 0; c < NV; ++c) partial[(long long)blockIdx.x * 4 + c] = v[c];
-        __threadfence();
-        unsigned prev = atomicAdd(counter, 1u);
-        is_last = (prev == (unsigned)(group_count - 1));
-    }
-    __syncthreads();
-    if (!is_last) return;
-    __threadfence();
-    float acc[NV];
-#pragma unroll
-    for (int c = 0; c < NV; ++c) acc[c] = 0.f;
-    const volatile float* vp = partial;
-    for (int b = threadIdx.x; b < group_count; b += blockDim.x)
-#pragma unroll
-        for (int c = 0; c < NV; ++c) acc[c] += vp[(long long)(group_first + b) * 4 + c];
-    block_reduce<NV>(acc, sh);
-    if (threadIdx.x == 0) {
-#pragma unroll
-        for (int c = 0; c < NV; ++c) out[c] = acc[c] * scale;
-        *counter = 0u;
-    }
-}
-
-__device__ __forceinline__ void red_add4(float4* p, float a, float b, float c, float d) {
-    atomicAdd(p, make_float4(a, b, c, d));
-}
-
-// ---------------------------------------------------------------------------
-// state loads
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ void load3(const float* st, long long stride, int o, long long p, float* v) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) v[c] = __ldg(st + (long long)(o + c) * stride + p);
-}
-__device__ __forceinline__ void load9(const float* st, long long stride, int o, long long p, float* v) {
-#pragma unroll
-    for (int c = 0; c < 9; ++c) v[c] = __ldg(st + (long long)(o + c) * stride + p);
-}
-__device__ __forceinline__ void store3(float* st, long long stride, int o, long long p, const float* v) {
-#pragma unroll
-    for (int c = 0; c < 3; ++c) st[(long long)(o + c) * stride + p] = v[c];
-}
-__device__ __forceinline__ void store9(float* st, long long stride, int o, long long p, const float* v) {
-#pragma unroll
-    for (int c = 0; c < 9; ++c) st[(long long)(o + c) * stride + p] = v[c];
-}
-
-// Stress and affine momentum of a liquid particle (p2g :111-152).
-struct LiquidP2G {
-    float Ft[9];
-    float A[9];
-    float vv[3];
-    float J;
-};
-
-__device__ __forceinline__ void liquid_p2g(const SceneDev& s, int model, const float* prm, const float* v,
-                                           const float* C, const float* F, LiquidP2G& o) {
-    float IC[9];
-#pragma unroll
-    for (int i = 0; i < 9; ++i) IC[i] = s.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
-    matmul3(IC, F, o.Ft);
-    if (s.j_mode == DSTIR_J_SVD) {
-        float U[9], sg[3], V[9];
-        svd3(o.Ft, U, sg, V);
-        o.J = sg[0] * sg[1] * sg[2];
-    } else {
-        o.J = det3(o.Ft);
-    }
-    float nrm2 = 0.f;
-#pragma unroll
-    for (int i = 0; i < 9; ++i) nrm2 += C[i] * C[i];
-    float gamma = sqrtf(nrm2) + 1e-6f;
-    Visc vs = viscosity<false>(model, prm, gamma);
-    float pr = (s.bulk / 2.f) * (o.J - (1.f / o.J) - 1.f) * o.J;
-#pragma unroll
-    for (int a = 0; a < 3; ++a)
-#pragma unroll
-        for (int b = 0; b < 3; ++b) {
-            float Dab = 0.5f * (C[a * 3 + b] + C[b * 3 + a]);
-            float sig = vs.eta * Dab + ((a == b) ? pr : 0.f);
-            o.A[a * 3 + b] = s.alpha * sig + s.m_liq * C[a * 3 + b];
-        }
-    o.vv[0] = v[0];
-    o.vv[1] = v[1] + s.dt * s.gravity;
-    o.vv[2] = v[2];
-}
-
-// ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
-template <int VARIANT>
+template <int VARIANT, bool SVDJ>
 __global__ void __launch_bounds__(256) p2g_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
@@ -168,7 +46,7 @@ __global__ void __launch_bounds__(256) p2g_kernel(FwdArgs a) {
 #pragma unroll
         for (int i = 0; i < 4; ++i) prm[i] = __ldg(a.params + bi.scene * 4 + i);
         LiquidP2G q;
-        liquid_p2g(s, __ldg(a.models + bi.scene), prm, v, C, F, q);
+        liquid_p2g<SVDJ>(s, __ldg(a.models + bi.scene), prm, v, C, F, q);
         store9(a.next, a.stride, OF, p, q.Ft);  // F[f+1] = F_tmp (:153)
         m = s.m_liq;
 #pragma unroll
@@ -537,6 +415,7 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(AdjArgs a) {
     a.pmb[node] = make_float4(inv_m * ub[0], inv_m * ub[1], inv_m * ub[2], mb - inv_m * inv_m * Pu);
 }
 
+template <bool SVDJ>
 __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
@@ -570,7 +449,7 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
 #pragma unroll
             for (int i = 0; i < 9; ++i) IC[i] = s.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
             matmul3(IC, F, Ft);
-            if (s.j_mode == DSTIR_J_SVD) {
+            if (SVDJ && s.j_mode == DSTIR_J_SVD) {
                 svd3(Ft, U, sg, Vm);
                 J = sg[0] * sg[1] * sg[2];
             } else {
@@ -679,7 +558,7 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
             float Jb = trb * (s.bulk / 2.f) * (2.f * J - 1.f);
             float Ftb[9];
             load9(a.adj_next, a.stride, OF, p, Ftb);  // F[f+1] = F_tmp
-            if (s.j_mode == DSTIR_J_SVD) {
+            if (SVDJ && s.j_mode == DSTIR_J_SVD) {
                 float gS[3] = {Jb * sg[1] * sg[2], Jb * sg[0] * sg[2], Jb * sg[0] * sg[1]};
                 float z[9], gA[9];
 #pragma unroll
@@ -773,12 +652,14 @@ __global__ void reduce_pgrad_kernel(const float* pgrad, int T, int B, float* out
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, cudaStream_t st) {
+void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st) {
     if (n_blocks <= 0) return;
     if (variant == P2G_PLAIN)
-        p2g_kernel<P2G_PLAIN><<<n_blocks, block, 0, st>>>(a);
+        svdj ? p2g_kernel<P2G_PLAIN, true><<<n_blocks, block, 0, st>>>(a)
+             : p2g_kernel<P2G_PLAIN, false><<<n_blocks, block, 0, st>>>(a);
     else
-        p2g_kernel<P2G_VEC><<<n_blocks, block, 0, st>>>(a);
+        svdj ? p2g_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
+             : p2g_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks > 0) grid_kernel<<<n_gblocks, gblock, 0, st>>>(a);
@@ -796,8 +677,12 @@ void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cuda
 void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks > 0) grid_adj_kernel<<<n_gblocks, gblock, 0, st>>>(a);
 }
-void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, cudaStream_t st) {
-    if (n_blocks > 0) p2g_adj_kernel<<<n_blocks, block, 0, st>>>(a);
+void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st) {
+    if (n_blocks <= 0) return;
+    if (svdj)
+        p2g_adj_kernel<true><<<n_blocks, block, 0, st>>>(a);
+    else
+        p2g_adj_kernel<false><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
                        long long stride, long long n, cudaStream_t s) {

@@ -64,8 +64,13 @@ def fixture_scene(name, model):
                  d['operator_trajectory'], d['m%d_params' % model]), d
 
 
+VARIANTS = [{'p2g': 1}, {'p2g': 2}, {'p2g': 2, 'graph': 1}]
+VARIANT_IDS = ['vec-atomics', 'binned', 'binned-graph']
+
+
+@pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
 @pytest.mark.parametrize('model', [0, 1, 2])
-def test_reference_scene_golden(model):
+def test_reference_scene_golden(model, opts):
     """Reference scene (container, rod particles, k=20000) built by the
     reference's own code: GPU vs the FP64 oracle and vs the reference's
     compute_loss gradient."""
@@ -74,7 +79,7 @@ def test_reference_scene_golden(model):
     T = sc.n_steps
     force_o, _, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, sc.x0())
     loss, dF = gu.reference_loss_and_dforce(force_o, d['m%d_target' % model], T)
-    force_g, dp_g, _, st = gpu_force_and_grad(sc, T, dF)
+    force_g, dp_g, _, st = gpu_force_and_grad(sc, T, dF, options=opts)
     assert st == 0
     _, dp_o, _ = oracle_force_and_grad(sc, T, dF)
     assert rel(force_g, force_o) < FORCE_RTOL
@@ -87,12 +92,13 @@ def test_reference_scene_golden(model):
                                           (S.MODEL_CARREAU, (2.0, 0.1, 0.6, 0.8)),
                                           (S.MODEL_CROSS, (1.5, 0.2, 0.5, 1.2))])
 @pytest.mark.parametrize('j_mode', [S.J_DET, S.J_SVD])
-def test_cylinder_scene_parity(model, params, j_mode):
+@pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
+def test_cylinder_scene_parity(model, params, j_mode, opts):
     T = 40
     sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, params=params, model=model,
                                          j_mode=j_mode, seed=1))
     wts = np.random.default_rng(0).normal(size=(T, 3))
-    force_g, dp_g, ds_g, st = gpu_force_and_grad(sc, T, wts, ckpt=7, want_state0=True)
+    force_g, dp_g, ds_g, st = gpu_force_and_grad(sc, T, wts, ckpt=7, want_state0=True, options=opts)
     assert st == 0
     force_o, dp_o, ds_o = oracle_force_and_grad(sc, T, wts, want_state0=True)
     assert rel(force_g, force_o) < FORCE_RTOL
@@ -130,9 +136,32 @@ def test_p2g_variants_agree():
     sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=5))
     wts = np.random.default_rng(4).normal(size=(T, 3))
     f0, g0, _, _ = gpu_force_and_grad(sc, T, wts, options={'p2g': 0})
-    f1, g1, _, _ = gpu_force_and_grad(sc, T, wts, options={'p2g': 1})
-    assert rel(f1, f0) < 1e-5
-    assert rel(g1, g0) < 1e-4
+    for opts in ({'p2g': 1}, {'p2g': 2}, {'p2g': 2, 'block': 128, 'gblock': 128}, {'p2g': 1, 'graph': 1}):
+        f1, g1, _, _ = gpu_force_and_grad(sc, T, wts, options=opts)
+        assert rel(f1, f0) < 1e-5, opts
+        assert rel(g1, g0) < 1e-4, opts
+
+
+def test_graph_replay_matches_eager_and_is_reusable():
+    T = 18
+    sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=7))
+    wts = torch.as_tensor(np.random.default_rng(8).normal(size=(1, T, 3)), dtype=torch.float32, device='cuda')
+    eager = Simulator(sc, max_steps=T, options={'p2g': 2})
+    graph = Simulator(sc, max_steps=T, options={'p2g': 2, 'graph': 1})
+    fe = eager.forward(T, ckpt_every=5, record=True)
+    ge = eager.backward(wts)
+    for rep in range(3):  # replays of the cached graphs with new parameters
+        p = torch.tensor(sc.params[None] * (1 + 0.1 * rep), dtype=torch.float32, device='cuda')
+        for sim in (eager, graph):
+            sim.set_params(p)
+            sim.reset()
+        fe = eager.forward(T, ckpt_every=5, record=True)
+        ge = eager.backward(wts)
+        fg = graph.forward(T, ckpt_every=5, record=True)
+        gg = graph.backward(wts)
+        torch.cuda.synchronize()
+        assert rel(fg.cpu().numpy(), fe.cpu().numpy()) < 1e-5
+        assert rel(gg.cpu().numpy(), ge.cpu().numpy()) < 1e-4
 
 
 def test_batched_equals_single():
@@ -145,13 +174,14 @@ def test_batched_equals_single():
                                  (1, 0.42, (2.0, 0.1, 0.6, 0.8), S.MODEL_CARREAU),
                                  (2, 0.22, (0.9, 0.4, 0.8, 0.0), S.MODEL_HB))]
     wts = np.random.default_rng(5).normal(size=(len(scenes), T, 3))
-    sim = Simulator(scenes, max_steps=T)
-    force = sim.forward(T, ckpt_every=6, record=True).cpu().numpy()
-    dp = sim.backward(torch.as_tensor(wts, dtype=torch.float32, device='cuda')).cpu().numpy()
-    for b, sc in enumerate(scenes):
-        f1, g1, _, _ = gpu_force_and_grad(sc, T, wts[b], ckpt=6)
-        assert rel(force[b], f1) < 1e-5
-        assert rel(dp[b], g1) < 1e-4
+    for opts in ({'p2g': 1}, {'p2g': 2, 'graph': 1}):
+        sim = Simulator(scenes, max_steps=T, options=opts)
+        force = sim.forward(T, ckpt_every=6, record=True).cpu().numpy()
+        dp = sim.backward(torch.as_tensor(wts, dtype=torch.float32, device='cuda')).cpu().numpy()
+        for b, sc in enumerate(scenes):
+            f1, g1, _, _ = gpu_force_and_grad(sc, T, wts[b], ckpt=6)
+            assert rel(force[b], f1) < 1e-5
+            assert rel(dp[b], g1) < 1e-4
 
 
 def test_reference_scene_rod_particles_71():
@@ -205,15 +235,17 @@ def test_svd_kernels_match_oracle():
     assert np.median(err) < 1e-4 and np.max(err) < 1e-2
 
 
-def test_out_of_grid_particle_sets_status_and_is_skipped():
+@pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
+def test_out_of_grid_particle_sets_status_and_is_skipped(opts):
     T = 4
     sc = S.small_synthetic_scene(n_grid=16, ppc=1, n_steps=T, seed=0)
     x = sc.x0()
     x[0] = (-0.5, 0.5, 0.5)   # base < 0
     x[1] = (2.0, 0.5, 0.5)    # base > n-3
     sc.liquid_x = x
-    sim = Simulator(sc, max_steps=T)
-    sim.forward(T)
+    sim = Simulator(sc, max_steps=T, options=opts)
+    sim.forward(T, record=True, ckpt_every=2)
+    sim.backward(torch.ones((1, T, 3), device='cuda'))
     torch.cuda.synchronize()
     flags = sim.status()
     assert flags & 2
