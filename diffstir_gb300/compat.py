@@ -186,6 +186,7 @@ class _PositionHistory:
 
     def to_numpy(self):
         _ensure_sim()
+        _flush_pending(record=_state.tape is not None)
         _materialize_positions()
         h = _state.hist_x  # torch [max_steps, N, 3]
         sc = _sc
@@ -196,6 +197,7 @@ class _PositionHistory:
 
 class _TotalDv:
     def to_numpy(self):
+        _flush_pending(record=_state.tape is not None)
         return _state.total_dv.copy()
 
     def __getitem__(self, k):
@@ -263,38 +265,41 @@ def initialize_ti_field():
 
 
 def forward(s):
-    """One substep (simulation_functions.py:341-348)."""
+    """One substep (simulation_functions.py:341-348).  Consecutive calls are
+    gathered and run as one rollout when a result is needed (compute_loss,
+    to_numpy, the end of a tape)."""
     s = int(s)
-    if _state.tape is not None and not _state.tape.replaying:
-        if _state.pending and s != _state.pending[-1] + 1:
-            raise ValueError('forward(%d) inside a tape must follow forward(%d)' % (s, _state.pending[-1]))
-        _state.pending.append(s)
-        return
-    sim = _ensure_sim()
-    _push_params()
-    f = sim.substep(s)
-    _state.forces[s + 1] = f[0].cpu().numpy()
-    _state.hist_x[s + 1] = sim.get_state()['x']
+    if _state.pending and s != _state.pending[-1] + 1:
+        _flush_pending(record=False)
+    _state.pending.append(s)
 
 
 def _flush_pending(record):
     if not _state.pending:
         return
+    import torch
     sim = _ensure_sim()
     _push_params()
     t0, n = _state.pending[0], len(_state.pending)
-    st0 = sim.get_state()
-    force = sim.forward(n, t0=t0, ckpt_every=max(1, int(math.isqrt(n))), record=record)
+    _state.pending = []
+    if record:
+        st0 = sim.get_state()
+        force = sim.forward(n, t0=t0, ckpt_every=max(1, int(math.isqrt(n))), record=True)
+        _state.rec = (t0, n)
+        # positions of frames t0+1..t0+n are produced on demand (to_numpy) by
+        # replaying from the saved start state on a second handle, so that the
+        # recorded checkpoints of `sim` stay intact for the adjoint
+        _state.hist_pending = (st0, t0, n, constitutive_parameters.to_numpy().copy(), int(model_index[None]),
+                               _sc.trajectory.copy())
+    else:
+        _materialize_positions()
+        force = torch.empty((1, n, 3), device=sim.device)
+        for i in range(n):
+            force[:, i] = sim.substep(t0 + i)
+            _state.hist_x[t0 + i + 1] = sim.get_state()['x']
     fo = force[0].cpu().numpy()
     for i in range(n):
         _state.forces[t0 + i + 1] = fo[i]
-    _state.rec = (t0, n)
-    # positions of frames t0+1..t0+n are produced on demand (to_numpy) by
-    # replaying from the saved start state on a second handle, so that the
-    # recorded checkpoints of `sim` stay intact for the adjoint
-    _state.hist_pending = (st0, t0, n, constitutive_parameters.to_numpy().copy(), int(model_index[None]),
-                           _sc.trajectory.copy())
-    _state.pending = []
 
 
 def _materialize_positions():
@@ -347,8 +352,8 @@ class _Tape:
     def __enter__(self):
         if self.clear:
             constitutive_parameters.grad.fill(0)
+        _flush_pending(record=False)
         _state.tape = self
-        _state.pending = []
         return self
 
     def __exit__(self, et, ev, tb):

@@ -415,70 +415,55 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(AdjArgs a) {
     a.pmb[node] = make_float4(inv_m * ub[0], inv_m * ub[1], inv_m * ub[2], mb - inv_m * inv_m * Pu);
 }
 
+// P2G adjoint in three phases so that few values stay live across the 27-node
+// gather: (1) recompute the particle's affine momentum A and m*v' (as in the
+// forward), (2) gather the P/M adjoint over the stencil, (3) reload C and F and
+// run the stress / bulk / viscosity / F_tmp adjoints.
 template <bool SVDJ>
 __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
+    __shared__ float prm[4];
+    __shared__ int model;
     if (threadIdx.x == 0) {
         bi = a.blk[blockIdx.x];
         s = a.sc[bi.scene];
+        for (int i = 0; i < 4; ++i) prm[i] = a.params[bi.scene * 4 + i];
+        model = a.models[bi.scene];
     }
     __syncthreads();
     long long p = bi.start + threadIdx.x;
     bool active = p < bi.end;
     float pg[4] = {0.f, 0.f, 0.f, 0.f};
     if (active) {
-        float x[3], v[3], C[9];
-        load3(a.cur, a.stride, OX, p, x);
-        load3(a.cur, a.stride, OV, p, v);
-        load9(a.cur, a.stride, OC, p, C);
         const bool liquid = bi.kind == KIND_LIQUID;
-        float m, vv[3], A[9];
-        float F[9], IC[9], Ft[9], J = 1.f, nrm = 0.f, pr = 0.f;
-        float U[9], sg[3], Vm[9];
-        float prm[4];
-        Visc vs;
-        vs.eta = 0.f;
-        int model = 0;
-        if (liquid) {
-            load9(a.cur, a.stride, OF, p, F);
+        float x[3];
+        load3(a.cur, a.stride, OX, p, x);
+        float m, mv[3], A[9];
+        {  // phase 1
+            float v[3], C[9];
+            load3(a.cur, a.stride, OV, p, v);
+            load9(a.cur, a.stride, OC, p, C);
+            if (liquid) {
+                float F[9];
+                load9(a.cur, a.stride, OF, p, F);
+                LiquidP2G q;
+                liquid_p2g<SVDJ>(s, model, prm, v, C, F, q);
+                m = s.m_liq;
 #pragma unroll
-            for (int i = 0; i < 4; ++i) prm[i] = __ldg(a.params + bi.scene * 4 + i);
-            model = __ldg(a.models + bi.scene);
+                for (int i = 0; i < 9; ++i) A[i] = q.A[i];
 #pragma unroll
-            for (int i = 0; i < 9; ++i) IC[i] = s.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
-            matmul3(IC, F, Ft);
-            if (SVDJ && s.j_mode == DSTIR_J_SVD) {
-                svd3(Ft, U, sg, Vm);
-                J = sg[0] * sg[1] * sg[2];
+                for (int c = 0; c < 3; ++c) mv[c] = m * q.vv[c];
             } else {
-                J = det3(Ft);
+                m = (bi.kind == KIND_ROD) ? s.m_rod : s.m_cont;
+#pragma unroll
+                for (int i = 0; i < 9; ++i) A[i] = m * C[i];
+#pragma unroll
+                for (int c = 0; c < 3; ++c) mv[c] = m * v[c];
             }
-            float nrm2 = 0.f;
-#pragma unroll
-            for (int i = 0; i < 9; ++i) nrm2 += C[i] * C[i];
-            nrm = sqrtf(nrm2);
-            vs = viscosity<true>(model, prm, nrm + 1e-6f);
-            pr = (s.bulk / 2.f) * (J - (1.f / J) - 1.f) * J;
-            m = s.m_liq;
-#pragma unroll
-            for (int aa = 0; aa < 3; ++aa)
-#pragma unroll
-                for (int bb = 0; bb < 3; ++bb) {
-                    float Dab = 0.5f * (C[aa * 3 + bb] + C[bb * 3 + aa]);
-                    A[aa * 3 + bb] = s.alpha * (vs.eta * Dab + ((aa == bb) ? pr : 0.f)) + m * C[aa * 3 + bb];
-                }
-            vv[0] = v[0];
-            vv[1] = v[1] + s.dt * s.gravity;
-            vv[2] = v[2];
-        } else {
-            m = (bi.kind == KIND_ROD) ? s.m_rod : s.m_cont;
-#pragma unroll
-            for (int i = 0; i < 9; ++i) A[i] = m * C[i];
-#pragma unroll
-            for (int c = 0; c < 3; ++c) vv[c] = v[c];
         }
+        // phase 2: gather of the P/M adjoint
         float Ab[9], vvb[3] = {0.f, 0.f, 0.f}, fxb[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int i = 0; i < 9; ++i) Ab[i] = 0.f;
@@ -487,7 +472,6 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
         if (locate(x, s.inv_dx, s.n, base, fx)) {
             float w[3][3], dw[3][3];
             bspline_d(fx, w, dw);
-            float mv[3] = {m * vv[0], m * vv[1], m * vv[2]};
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
@@ -505,7 +489,7 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
                         for (int aa = 0; aa < 3; ++aa) {
                             float ad = A[aa * 3 + 0] * dp[0] + A[aa * 3 + 1] * dp[1] + A[aa * 3 + 2] * dp[2];
                             Wb += gbv[aa] * (mv[aa] + ad);
-                            vvb[aa] += W * m * gbv[aa];
+                            vvb[aa] += W * gbv[aa];
 #pragma unroll
                             for (int bb = 0; bb < 3; ++bb) Ab[aa * 3 + bb] += W * gbv[aa] * dp[bb];
                         }
@@ -521,25 +505,46 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
                     }
                 }
         }
-        float Cb[9];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) vvb[c] *= m;
+        // phase 3
         if (!liquid) {
+            float Cb[9], z[9];
 #pragma unroll
-            for (int i = 0; i < 9; ++i) Cb[i] = m * Ab[i];
-            float z[9];
-#pragma unroll
-            for (int i = 0; i < 9; ++i) z[i] = 0.f;
+            for (int i = 0; i < 9; ++i) {
+                Cb[i] = m * Ab[i];
+                z[i] = 0.f;
+            }
             store3(a.adj_cur, a.stride, OX, p, z);
             store3(a.adj_cur, a.stride, OV, p, z);
             store9(a.adj_cur, a.stride, OC, p, Cb);
             store9(a.adj_cur, a.stride, OF, p, z);
         } else {
             float xb[3];
-            load3(a.adj_cur, a.stride, OX, p, xb);  // G2P part, written by g2p_adj_kernel
+            load3(a.adj_cur, a.stride, OX, p, xb);  // G2P part, written by the G2P adjoint
 #pragma unroll
             for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
             store3(a.adj_cur, a.stride, OX, p, xb);
             store3(a.adj_cur, a.stride, OV, p, vvb);
-            float sigb[9];
+            float C[9], F[9], IC[9], Ft[9];
+            load9(a.cur, a.stride, OC, p, C);
+            load9(a.cur, a.stride, OF, p, F);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) IC[i] = s.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
+            matmul3(IC, F, Ft);
+            float U[9], sg[3], Vm[9], J;
+            if (SVDJ && s.j_mode == DSTIR_J_SVD) {
+                svd3(Ft, U, sg, Vm);
+                J = sg[0] * sg[1] * sg[2];
+            } else {
+                J = det3(Ft);
+            }
+            float nrm2 = 0.f;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) nrm2 += C[i] * C[i];
+            float nrm = sqrtf(nrm2);
+            Visc vs = viscosity<true>(model, prm, nrm + 1e-6f);
+            float Cb[9], sigb[9];
 #pragma unroll
             for (int i = 0; i < 9; ++i) {
                 Cb[i] = m * Ab[i];

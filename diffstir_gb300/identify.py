@@ -1,0 +1,136 @@
+"""Viscosity-parameter identification on top of the batched simulator.
+
+* :func:`adam_identify` runs R random restarts of Adam as ONE batched handle
+  (scene replicated R times, one parameter candidate per replica).  Every
+  iteration is a single checkpointed forward + adjoint of all R candidates.
+* :func:`single_parameter_fitting1` / :func:`magnitude_level` restate the
+  reference's magnitude-scaled step rule
+  (src/gradient_descent_module.py:3-42), so the reference's driver loop can be
+  reproduced on top of :class:`~diffstir_gb300.simulator.Simulator`.
+"""
+
+import copy
+import math
+import time
+
+import numpy as np
+import torch
+
+from .simulator import Simulator
+
+# (K, tau_y, n) bounds of the Herschel-Bulkley identification workload
+HB_BOUNDS = {0: (0.1, 2.0), 1: (0.0, 5.0), 2: (0.4, 1.2)}
+
+
+def force_mse(force, target):
+    """Mean squared error of the rod x and z force profiles, per scene [B]."""
+    d = (force - target)[..., 0::2]
+    return (d * d).mean(dim=(1, 2))
+
+
+def adam_identify(scene, target, restarts=16, iters=200, lr=1e-2, ckpt_every=50, free=(0, 1, 2), bounds=None,
+                  seed=0, options=None, log_every=0, callback=None):
+    """Fit the parameters ``free`` of ``scene`` to ``target`` [T,3] (or [1,T,3]).
+
+    Parameters are optimised in normalised form u in [0,1] (p = lo + u (hi-lo))
+    with torch.optim.Adam(lr), clamped to the box after each step.  Returns a
+    dict with the best parameters per restart, the overall best, the loss
+    history [iters, R] and the wall time."""
+    bounds = dict(HB_BOUNDS if bounds is None else bounds)
+    T = scene.n_steps
+    R = int(restarts)
+    scenes = [copy.copy(scene) for _ in range(R)]
+    sim = Simulator(scenes, max_steps=T, options=options)
+    dev = sim.device
+    tgt = torch.as_tensor(np.asarray(target), dtype=torch.float32, device=dev).reshape(1, T, 3).expand(R, T, 3)
+    rng = np.random.default_rng(seed)
+    free = list(free)
+    lo = torch.tensor([bounds[i][0] for i in free], device=dev)
+    hi = torch.tensor([bounds[i][1] for i in free], device=dev)
+    u = torch.tensor(rng.uniform(0.05, 0.95, size=(R, len(free))), dtype=torch.float32, device=dev,
+                     requires_grad=True)
+    base = torch.as_tensor(np.asarray(scene.params), dtype=torch.float32, device=dev).reshape(1, 4).repeat(R, 1)
+    opt = torch.optim.Adam([u], lr=lr)
+    hist = np.zeros((iters, R))
+    best_loss = np.full(R, np.inf)
+    best_p = base.clone()
+    t0 = time.perf_counter()
+    for it in range(iters):
+        opt.zero_grad()
+        p = base.clone()
+        p[:, free] = lo + u * (hi - lo)
+        force = sim.rollout(p, nsteps=T, ckpt_every=ckpt_every)
+        per = force_mse(force, tgt)
+        per.sum().backward()
+        opt.step()
+        with torch.no_grad():
+            u.clamp_(0.0, 1.0)
+        lv = per.detach().cpu().numpy()
+        hist[it] = lv
+        better = lv < best_loss
+        if better.any():
+            best_loss = np.where(better, lv, best_loss)
+            idx = torch.as_tensor(np.nonzero(better)[0], device=dev)
+            best_p[idx] = p.detach()[idx]
+        if log_every and (it % log_every == 0 or it == iters - 1):
+            print('iter %4d  loss min %.4e  median %.4e' % (it, lv.min(), np.median(lv)), flush=True)
+        if callback is not None:
+            callback(it, p.detach(), lv)
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t0
+    bp = best_p.cpu().numpy()
+    k = int(np.argmin(best_loss))
+    return {'best_params': bp, 'best_loss': best_loss, 'best': bp[k], 'best_index': k, 'history': hist,
+            'wall_s': wall, 'grad_evals': iters * R, 'sim': sim}
+
+
+# ---------------------------------------------------------------------------
+# the reference's step rule (src/gradient_descent_module.py:3-42)
+# ---------------------------------------------------------------------------
+def magnitude_level(a):
+    """floor(log10(max(|a|, 1e-11))), NaN -> 0 (gradient_descent_module.py:3-9)."""
+    abs_a = max(abs(a), 1e-11)
+    lg = math.log10(abs_a)
+    if np.isnan(lg):
+        lg = 0
+    return math.floor(lg)
+
+
+def single_parameter_fitting1(parameter, parameter_grad, lower_bound, upper_bound, lr, epochs, epoch_index):
+    """One magnitude-scaled step of one parameter (gradient_descent_module.py:11-42).
+
+    Returns (new parameter, new learning rate).  Differences from the
+    reference: the parameter, bounds and rate are passed in instead of being
+    read from module fields, and the bound-halving loop gives up after 2000
+    halvings (the reference loops until the step underflows when the bounds
+    coincide)."""
+    period = epochs - epoch_index
+    base = 3
+    if abs(parameter_grad) > 0:
+        delta = lr * parameter_grad
+        new_magnitude = 0
+        if parameter_grad < 0:
+            new_magnitude = magnitude_level((upper_bound - parameter) / period)
+        if parameter_grad > 0:
+            new_magnitude = magnitude_level((lower_bound - parameter) / period)
+        if epoch_index < 1:
+            lr *= pow(base, new_magnitude - magnitude_level(delta))
+            delta = lr * parameter_grad
+        parameter_update = parameter - delta
+        if lower_bound < parameter_update < upper_bound:
+            parameter = parameter_update
+            lr *= pow(base, new_magnitude - magnitude_level(delta))
+        else:
+            if parameter_update < lower_bound:
+                new_magnitude = magnitude_level((upper_bound - parameter) / period)
+            if parameter_update > upper_bound:
+                new_magnitude = magnitude_level((lower_bound - parameter) / period)
+            lr *= pow(base, new_magnitude - magnitude_level(delta))
+            parameter_update = parameter - lr * parameter_grad
+            n = 0
+            while (parameter_update > upper_bound or parameter_update < lower_bound) and n < 2000:
+                lr *= 0.5
+                parameter_update = parameter - lr * parameter_grad
+                n += 1
+            parameter = parameter_update
+    return parameter, lr

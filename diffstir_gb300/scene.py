@@ -135,8 +135,12 @@ def reference_constants(args=None, n_liquid=None, n_rod=None, n_container=None, 
     return c
 
 
-def sample_reference_particles(c, traj_processed, seed):
-    """Rejection sampler of initialization.py:79-117 on a seeded RandomState."""
+def sample_reference_particles(c, rod_offset, seed):
+    """Rejection sampler of initialization.py:79-117 on a seeded RandomState.
+
+    ``rod_offset`` is the reference's ``initial_pos_related_to_center``
+    (initialization.py:78): the first frame of the already-centred trajectory
+    minus the trajectory centre once more (see :func:`rod_offset`)."""
     rs = np.random.RandomState(seed)
     dx = c['dx']
     R, wt = c['container_radius'], c['container_wall_thickness']
@@ -178,11 +182,15 @@ def sample_reference_particles(c, traj_processed, seed):
     container = np.array(container).reshape(-1, 3) + centre
     liquid = np.array(liquid).reshape(-1, 3) + centre
     rod = np.array(rod).reshape(-1, 3) + centre
-    # initialization.py:75-78,117: offset of the first frame from the box centre
-    t = traj_processed
-    tc = (np.amax(t, axis=0) - np.amin(t, axis=0)) / 2 + np.amin(t, axis=0)
-    rod = rod + (t[0] - tc)
+    rod = rod + np.asarray(rod_offset)
     return liquid, rod, container
+
+
+def rod_offset(traj_processed, centre):
+    """initialization.py:78: ``operator_trajectory[0] - operator_trajectory_center``
+    evaluated after the trajectory was already centred (:77), i.e. the centre
+    is subtracted twice; kept as the reference computes it."""
+    return np.asarray(traj_processed)[0] - np.asarray(centre)
 
 
 def reference_desc(c, model=MODEL_CARREAU, j_mode=J_DET):
@@ -225,8 +233,8 @@ def reference_scene(seed=0, n_steps=None, raw_trajectory=None, model=MODEL_CARRE
     if n_steps is not None:
         raw = raw[:n_steps + 1]
     c = reference_constants(args, n_liquid, n_rod, n_container, n_grid)
-    traj, _ = process_trajectory(raw)
-    liquid, rod, container = sample_reference_particles(c, traj, seed)
+    traj, centre = process_trajectory(raw)
+    liquid, rod, container = sample_reference_particles(c, rod_offset(traj, centre), seed)
     desc = reference_desc(c, model, j_mode)
     return Scene(desc, liquid, rod, container, traj, np.asarray(params, dtype=np.float64),
                  info={'kind': 'reference', 'seed': seed, 'constants': c})

@@ -115,6 +115,7 @@ def run_fixture(ref_root, name, n_grid, n_liq, n_op, n_cont, T, seed, prec, mode
         sf = load_reference(ref_root, cfg, traj, force, seed, prec)
         if not out:
             out.update(scene_record(sf))
+            out['raw_trajectory'] = traj.copy()
         params = MODEL_PARAMS[model]
         sf.model_index[None] = model
         for j in range(4):
