@@ -68,6 +68,7 @@ PROTOTYPES = {
     'dstir_get_option': (C.c_int, [P, C.c_char_p, C.POINTER(C.c_int64)]),
     'dstir_svd3': (C.c_int, [P, P, P, P, C.c_int64, P]),
     'dstir_svd3_backward': (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P]),
+    'dstir_substep_static': (C.c_int, [C.POINTER(DstirSceneDesc), P, P, P, P, P, P]),
 }
 
 

@@ -154,6 +154,25 @@ int dstir_svd3(const float* A, float* U, float* S, float* V, int64_t n, void* st
 int dstir_svd3_backward(const float* gU, const float* gS, const float* gV, const float* U,
                         const float* S, const float* V, float* gA, int64_t n, void* stream);
 
+/* One substep of one scene that allocates no device memory.  No counterpart in
+ * the reference: it exists for callers that may not call cudaMalloc (a host
+ * framework that owns the device pool and forbids allocations in its
+ * callbacks, or a stepping loop that cannot take the synchronisation an
+ * allocation may cause).  It runs the same kernels as dstir_substep, with its
+ * grids, tables and reduction scratch in one static device array of about
+ * 8.3 MB that every GPU loading the library keeps until exit.
+ *  - scene: one descriptor (host pointer); n = n_liquid + n_rod + n_container.
+ *  - params [4], traj2 [2][3] (rod reference point at frames f and f+1),
+ *    state_in / state_out [24][n] (component-major: x0..2 v0..2 C00..C22
+ *    F00..F22, component c of particle p at c*n + p; must not overlap),
+ *    force_out [3] (the substep's rod reaction force): device pointers.
+ *  - Limits: n_grid <= 64 and n <= 1048576, else DSTIR_ERANGE.
+ *  - Calls share the static array: calls that overlap on the GPU race; the
+ *    first call on a device looks the array up and should precede any stream
+ *    capture.  Device status flags are not reported. */
+int dstir_substep_static(const DstirSceneDesc* scene, const float* params, const float* traj2,
+                         const float* state_in, float* state_out, float* force_out, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
