@@ -58,10 +58,12 @@ def parse():
     ap.add_argument('--config', default='C2')
     ap.add_argument('--substeps', type=int, default=None, help='override the substep count')
     ap.add_argument('--ckpt', type=int, default=None)
+    ap.add_argument('--batch', type=int, default=None, help='scenes per GPU (default: the configuration\'s)')
     ap.add_argument('--p2g', type=int, default=None, help='0 scalar atomics, 1 vector atomics, 2 binned cells')
     ap.add_argument('--graph', type=int, default=None, help='1: replay rollouts as CUDA graphs')
     ap.add_argument('--block', type=int, default=None)
     ap.add_argument('--gblock', type=int, default=None)
+    ap.add_argument('--autotune', type=int, default=1, help='1: launch options from the autotuner (cached)')
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')
@@ -146,18 +148,33 @@ def ncu_traffic(kernel, workload):
 
 
 def build_workload(args, rank):
+    """Scenes of this rank: one for the single-scene configurations, ``batch``
+    seeded scenes (uneven fill heights) for the batched one."""
     from diffstir_gb300 import scene as S
     cfg = S.CONFIGS[args.config]
     T = args.substeps or cfg['n_steps']
-    sc = S.synthetic_scene(args.config, seed=rank, n_steps=T)
+    B = args.batch or cfg.get('batch', 1)
+    scenes = [S.synthetic_scene(args.config, seed=rank * B + b, n_steps=T) for b in range(B)]
     ckpt = args.ckpt or cfg['ckpt']
-    return sc, T, ckpt
+    return scenes, T, ckpt
 
 
-def workload_name(args, sc, T, ckpt):
-    d = sc.desc
-    return ('%s: %d^3 grid, %d particles (8/cell), %d substeps, checkpoint every %d, power-law fluid, '
-            'moving cylinder rod; forward + checkpointed adjoint' % (args.config, d.n_grid, sc.n_particles, T, ckpt))
+def workload_name(args, scenes, T, ckpt):
+    d = scenes[0].desc
+    N = sum(s.n_particles for s in scenes)
+    visc = 'Herschel-Bulkley fluid' if S_yield(args.config) else 'power-law fluid'
+    if len(scenes) == 1:
+        return ('%s: %d^3 grid, %d particles (8/cell), %d substeps, checkpoint every %d, %s, '
+                'moving cylinder rod; forward + checkpointed adjoint' % (args.config, d.n_grid, N, T, ckpt, visc))
+    return ('%s: %d scenes of %d^3 grid, %d particles in all (%d..%d per scene), %d substeps, checkpoint every %d, '
+            '%s, moving cylinder rod; batched forward + checkpointed adjoint' %
+            (args.config, len(scenes), d.n_grid, N, min(s.n_particles for s in scenes),
+             max(s.n_particles for s in scenes), T, ckpt, visc))
+
+
+def S_yield(config):
+    from diffstir_gb300 import scene as S
+    return bool(S.CONFIGS[config].get('yield_stress', False))
 
 
 # ---------------------------------------------------------------------------
@@ -178,7 +195,8 @@ def run_reference(args):
         return 0
     import oracle
     oracle.build()
-    sc, T, ckpt = build_workload(args, 0)
+    scenes, T, ckpt = build_workload(args, 0)
+    sc = scenes[0]
     threads = os.cpu_count() or 1
     Ts = min(args.ref_sample, T)
     for _ in range(args.warmup):
@@ -191,9 +209,9 @@ def run_reference(args):
         'warmup': args.warmup, 'ms_per_step': dt * 1e3, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
         'impl': 'reference',
-        'config': {'workload': workload_name(args, sc, T, ckpt), 'parallelism': 'host threads'},
+        'config': {'workload': workload_name(args, scenes, T, ckpt), 'parallelism': 'host threads'},
         'cpu_baseline': {'value': val, 'unit': UNIT, 'cores': threads, 'kind': 'port',
-                         'sample': 'first %d of %d substeps, forward + adjoint, per step' % (Ts, T)},
+                         'sample': 'first %d of %d substeps of scene 0, forward + adjoint, per step' % (Ts, T)},
         'e2e': {'value': val, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0},
         'note': 'the reference is a Taichi program (Taichi is not installable offline); its CPU path is '
                 'timed through the line-by-line C++ restatement oracle/oracle.cpp (FP32, OpenMP)',
@@ -213,21 +231,29 @@ def run_ours(args):
     from diffstir_gb300.simulator import Simulator
     from diffstir_gb300 import scene as S
 
-    sc, T, ckpt = build_workload(args, rank)
+    scenes, T, ckpt = build_workload(args, rank)
+    sc = scenes[0]
     opts = {}
+    explicit = any(getattr(args, k) is not None for k in ('p2g', 'graph', 'block', 'gblock'))
+    if args.autotune and not explicit:
+        from diffstir_gb300 import autotune
+        opts = autotune.autotune(scenes)
     for k in ('p2g', 'graph', 'block', 'gblock'):
         if getattr(args, k) is not None:
             opts[k] = getattr(args, k)
-    sim = Simulator(sc, max_steps=T, options=opts)
+    sim = Simulator(scenes, max_steps=T, options=opts)
     dev = torch.device('cuda', local)
-    N = sc.n_particles
+    N = sum(s.n_particles for s in scenes)
+    B = len(scenes)
+    rng = np.random.default_rng(1000 + rank)
+    ys = S_yield(args.config)
 
-    # target force profile from ground-truth parameters
-    true_p = torch.tensor(S.draw_params(np.random.default_rng(1000 + rank))[None], dtype=torch.float32, device=dev)
+    # target force profiles from seeded ground-truth parameters
+    true_p = torch.tensor(np.stack([S.draw_params(rng, ys) for _ in range(B)]), dtype=torch.float32, device=dev)
     sim.set_params(true_p)
     sim.reset()
     target = sim.forward(T).clone()
-    params = torch.tensor(sc.params[None], dtype=torch.float32, device=dev)
+    params = torch.tensor(np.stack([s.params for s in scenes]), dtype=torch.float32, device=dev)
 
     def grad_eval(p):
         sim.set_params(p)
@@ -284,11 +310,11 @@ def run_ours(args):
     # e2e through the public API with pinned host inputs / host results
     e2e = None
     if not args.no_e2e:
-        x0_h = torch.from_numpy(sc.x0()).float().pin_memory()
+        x0_h = torch.from_numpy(np.concatenate([s.x0() for s in scenes], 0)).float().pin_memory()
         p_h = params.cpu().pin_memory()
         tgt_h = target.cpu().pin_memory()
         h2d = x0_h.numel() * 4 + p_h.numel() * 4 + tgt_h.numel() * 4
-        d2h = 4 * 4 + 4
+        d2h = B * 4 * 4 + 4
 
         def e2e_step():
             x0_d = x0_h.to(dev, non_blocking=True)
@@ -324,15 +350,16 @@ def run_ours(args):
         return 0
 
     # roofline of the dominant kernel (by total time inside the timed region)
-    G = sc.desc.n_grid ** 3
+    G = sum(s.desc.n_grid ** 3 for s in scenes)
+    NL = sum(s.desc.n_liquid for s in scenes)
     dom = max((k for k in KERNEL_BYTES), key=lambda k: prof[k][0])
     tot_ms, cnt = prof[dom]
     avg_s = tot_ms / 1e3 / max(cnt, 1)
     bp, bn = KERNEL_BYTES[dom]
-    alg = bp * sc.desc.n_liquid + bn * G
+    alg = bp * NL + bn * G
     hbm, peak_kind = peaks()
     achieved = alg / avg_s / 1e9
-    wl = workload_name(args, sc, T, ckpt)
+    wl = workload_name(args, scenes, T, ckpt)
     roof = {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
             'frac': achieved / hbm, 'peak_kind': peak_kind, 'alg_bytes_per_launch': alg,
             'avg_launch_us': avg_s * 1e6, 'traffic': ncu_traffic(dom, args.config)}
@@ -345,18 +372,19 @@ def run_ours(args):
         threads = os.cpu_count() or 1
         Ts = min(args.cpu_sample, T)
         dt = cpu_sample(sc, Ts, threads)
-        cpu = {'value': N * Ts / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
-               'sample': 'oracle FP32 forward + adjoint of the first %d of %d substeps of the same scene' % (Ts, T)}
+        cpu = {'value': sc.n_particles * Ts / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+               'sample': 'oracle FP32 forward + adjoint of the first %d of %d substeps of scene 0 (%d particles)'
+                         % (Ts, T, sc.n_particles)}
 
     line = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
         'warmup': args.warmup, 'ms_per_step': ms, 'higher_is_better': True, 'scaling': 'weak',
         'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic',
         'config': {'workload': wl, 'grid': G, 'particles': N, 'substeps': T, 'ckpt_every': ckpt,
-                   'scenes_per_gpu': 1, 'parallelism': 'one scene per GPU (scene-sharded)',
+                   'scenes_per_gpu': B, 'parallelism': 'scene-sharded (%d scene(s) per GPU)' % B,
                    'l2': 'inputs larger than L2 (checkpoints + segment states ~%.1f GB per step)' %
                          ((T // ckpt + ckpt) * N * 96 / 1e9)},
-        'grad_evals_per_s': world * 1e3 / ms,
+        'grad_evals_per_s': world * B * 1e3 / ms,
         'forward_adjoint_roofline_frac': step_bytes / (ms / 1e3) / 1e9 / hbm,
         'roofline': roof,
         'kernel_time_share': kernel_share,

@@ -143,6 +143,12 @@ struct DstirHandle {
     int* perm = nullptr;        // [bin_slots][stride]
     long long bin_slots = 0;
     bool any_svd = false;
+    // brick-major binning (p2g variant P2G_BRICK)
+    long long nbins_brick = 0;  // sum over scenes of 64 * ceil(n/4)^3
+    long long nbins_max = 0;    // bins the bin arrays are sized for: max(G, nbins_brick)
+    std::vector<BrickInfo> bricks_h;
+    BrickInfo* bricks = nullptr;
+    int n_bricks = 0;
 
     Profiler prof;
     long long launches = 0;  // kernel launches issued since the counter was reset
@@ -306,26 +312,30 @@ void timed(DstirHandle* h, int kind, cudaStream_t st, Fn fn) {
 int ensure_bin_slots(DstirHandle* h, long long n) {
     if (n <= h->bin_slots) return DSTIR_OK;
     int rc;
+    const long long nb = h->nbins_max;
     if (!h->cnt) {
-        if ((rc = dalloc(h, &h->cnt, (size_t)(h->G + 1), "bin counts"))) return rc;
-        CUDA_TRY(h, cudaMemset(h->cnt, 0, (size_t)(h->G + 1) * sizeof(int)));
+        if ((rc = dalloc(h, &h->cnt, (size_t)(nb + 1), "bin counts"))) return rc;
+        CUDA_TRY(h, cudaMemset(h->cnt, 0, (size_t)(nb + 1) * sizeof(int)));
         if ((rc = dalloc(h, &h->bkey, (size_t)h->stride, "bin keys"))) return rc;
         if ((rc = dalloc(h, &h->brank, (size_t)h->stride, "bin ranks"))) return rc;
-        if ((rc = dalloc(h, &h->bsum, (size_t)bin_scan_blocks(h->G), "scan scratch"))) return rc;
+        if ((rc = dalloc(h, &h->bsum, (size_t)bin_scan_blocks(nb), "scan scratch"))) return rc;
     }
-    if ((rc = dalloc(h, &h->cell_start, (size_t)(n * (h->G + 2)), "cell starts"))) return rc;
+    if ((rc = dalloc(h, &h->cell_start, (size_t)(n * (nb + 2)), "cell starts"))) return rc;
     if ((rc = dalloc(h, &h->perm, (size_t)(n * h->stride), "bin permutation"))) return rc;
     h->bin_slots = n;
     return DSTIR_OK;
 }
 
-int* slot_cell_start(DstirHandle* h, int slot) { return h->cell_start + (size_t)slot * (h->G + 2); }
+bool binned(const DstirHandle* h) { return h->p2g_variant == P2G_CELL || h->p2g_variant == P2G_BRICK; }
+
+int* slot_cell_start(DstirHandle* h, int slot) { return h->cell_start + (size_t)slot * (h->nbins_max + 2); }
 int* slot_perm(DstirHandle* h, int slot) { return h->perm + (size_t)slot * h->stride; }
 
 // One forward substep.  With the binned variant the particles of `a.cur` are
 // counting-sorted into bin slot `bin_slot` first.
 void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot = 0) {
-    if (h->p2g_variant == P2G_CELL) {
+    if (binned(h)) {
+        const bool brick = h->p2g_variant == P2G_BRICK;
         BinArgs b;
         b.sc = h->sc;
         b.blk = h->blk;
@@ -337,13 +347,19 @@ void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot
         b.cell_start = slot_cell_start(h, bin_slot);
         b.perm = slot_perm(h, bin_slot);
         b.bsum = h->bsum;
-        b.G = h->G;
+        b.G = brick ? h->nbins_brick : h->G;
         b.status = h->status;
+        b.key_mode = brick ? 1 : 0;
         h->launches += 4;
         timed(h, K_BIN, st, [&] { launch_bin(b, h->n_blocks, h->block, st); });
-        timed(h, K_P2G, st, [&] {
-            launch_p2g_cell(a, b.cell_start, b.perm, h->n_gblocks, h->gblock, h->G, h->any_svd, st);
-        });
+        if (brick)
+            timed(h, K_P2G, st, [&] {
+                launch_p2g_brick(a, h->bricks, h->n_bricks, b.cell_start, b.perm, b.G, h->any_svd, st);
+            });
+        else
+            timed(h, K_P2G, st, [&] {
+                launch_p2g_cell(a, b.cell_start, b.perm, h->n_gblocks, h->gblock, h->G, h->any_svd, st);
+            });
     } else {
         timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st); });
     }
@@ -352,7 +368,12 @@ void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot
 }
 
 void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st, int bin_slot = 0) {
-    if (h->p2g_variant == P2G_CELL) {
+    if (h->p2g_variant == P2G_BRICK) {
+        timed(h, K_G2P_ADJ, st, [&] {
+            launch_g2p_adj_brick(a, h->bricks, h->n_bricks, slot_cell_start(h, bin_slot), slot_perm(h, bin_slot),
+                                 h->nbins_brick, st);
+        });
+    } else if (h->p2g_variant == P2G_CELL) {
         timed(h, K_G2P_ADJ, st, [&] {
             launch_g2p_adj_cell(a, slot_cell_start(h, bin_slot), slot_perm(h, bin_slot), h->n_gblocks, h->gblock,
                                 h->G, st);
@@ -405,6 +426,21 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
         sd.n_container = d.n_container;
         sd.p0 = p0;
         sd.goff = g0;
+        sd.nbr = (d.n_grid + 3) / 4;
+        sd.koff = h->nbins_brick;
+        for (int bi = 0; bi < sd.nbr; ++bi)
+            for (int bj = 0; bj < sd.nbr; ++bj)
+                for (int bk = 0; bk < sd.nbr; ++bk) {
+                    BrickInfo b;
+                    b.scene = s;
+                    b.bi = bi;
+                    b.bj = bj;
+                    b.bk = bk;
+                    b.key0 = sd.koff + (((long long)bi * sd.nbr + bj) * sd.nbr + bk) * 64;
+                    b.pad = 0;
+                    h->bricks_h.push_back(b);
+                }
+        h->nbins_brick += 64LL * sd.nbr * sd.nbr * sd.nbr;
         sd.dt = d.dt;
         sd.dx = 1.f / (float)d.n_grid;
         sd.inv_dx = (float)d.n_grid;
@@ -427,6 +463,8 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
     h->N = p0;
     h->stride = std::max<long long>((p0 + 31) / 32 * 32, 32);
     h->G = g0;
+    h->nbins_max = std::max(h->G, h->nbins_brick);
+    h->n_bricks = (int)h->bricks_h.size();
     int rc = DSTIR_OK;
     std::vector<int> models(batch);
     for (int s = 0; s < batch; ++s) models[s] = scenes[s].model;
@@ -444,12 +482,15 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
         (rc = dalloc(h, &h->dpbuf, (size_t)batch * 4, "parameter adjoint")) ||
         (rc = dalloc(h, &h->pgrad, (size_t)max_steps * batch * 4, "parameter gradients")) ||
         (rc = dalloc(h, &h->counters, (size_t)3 * batch, "counters")) ||
-        (rc = dalloc(h, &h->status, 1, "status")) || (rc = ensure_grid_slots(h, 1)) || (rc = build_tables(h))) {
+        (rc = dalloc(h, &h->status, 1, "status")) || (rc = dalloc(h, &h->bricks, h->bricks_h.size(), "bricks")) ||
+        (rc = ensure_grid_slots(h, 1)) || (rc = build_tables(h))) {
         std::string msg = h->err;
         dstir_destroy(h);
         return rc;
     }
     cudaError_t e = cudaMemcpy(h->sc, h->sc_h.data(), batch * sizeof(SceneDev), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+        e = cudaMemcpy(h->bricks, h->bricks_h.data(), h->bricks_h.size() * sizeof(BrickInfo), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(h->models, models.data(), batch * sizeof(int), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemset(h->counters, 0, 3 * batch * sizeof(unsigned));
     if (e == cudaSuccess) e = cudaMemset(h->status, 0, sizeof(unsigned));
@@ -479,7 +520,8 @@ void dstir_destroy(DstirHandle* h) {
     if (h->ev_out) cudaEventDestroy(h->ev_out);
     void* ptrs[] = {h->sc, h->blk, h->gblk, h->work, h->ckpt, h->seg, h->pm, h->vo, h->ga, h->pmb, h->adj,
                     h->traj, h->params, h->models, h->force_scratch, h->pgrad, h->partial, h->counters, h->status,
-                    h->cnt, h->bkey, h->brank, h->bsum, h->cell_start, h->perm, h->fbuf, h->dfbuf, h->dpbuf};
+                    h->cnt, h->bkey, h->brank, h->bsum, h->cell_start, h->perm, h->fbuf, h->dfbuf, h->dpbuf,
+                    h->bricks};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -616,7 +658,7 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
         if ((rc = dalloc(h, &h->ckpt, (size_t)nseg * slot_floats(h), "checkpoints"))) return rc;
         h->ckpt_slots = nseg;
     }
-    if (h->p2g_variant == P2G_CELL && (rc = ensure_bin_slots(h, 1))) return rc;
+    if (binned(h) && (rc = ensure_bin_slots(h, 1))) return rc;
     long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch, h->p2g_variant, h->block * 4096 + h->gblock};
     int final_slot = 0;
     rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want,
@@ -653,7 +695,7 @@ int dstir_substep(DstirHandle* h, int32_t f, float* force_out, void* stream) {
     cudaStream_t st = S(stream);
     h->recorded = false;
     int rc;
-    if (h->p2g_variant == P2G_CELL && (rc = ensure_bin_slots(h, 1))) return rc;
+    if (binned(h) && (rc = ensure_bin_slots(h, 1))) return rc;
     size_t sf = slot_floats(h);
     float* W[2] = {h->work, h->work + sf};
     float* force = force_out ? force_out : h->force_scratch;
@@ -745,7 +787,7 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
         h->seg_slots = K;
     }
     if ((rc = ensure_grid_slots(h, K))) return rc;
-    if (h->p2g_variant == P2G_CELL && (rc = ensure_bin_slots(h, K))) return rc;
+    if (binned(h) && (rc = ensure_bin_slots(h, K))) return rc;
     // dL/dforce [B][n][3] -> internal [B][max_steps][3]
     CUDA_TRY(h, cudaMemcpy2DAsync(h->dfbuf, (size_t)h->max_steps * 3 * sizeof(float), dL_dforce,
                                   (size_t)n * 3 * sizeof(float), (size_t)n * 3 * sizeof(float), (size_t)h->B,
@@ -778,7 +820,7 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream) {
 int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     if (!h || !key) return DSTIR_EINVAL;
     if (!strcmp(key, "p2g")) {
-        if (value < 0 || value > 2) return fail(h, DSTIR_EINVAL, "p2g variant %lld not in 0..2", (long long)value);
+        if (value < 0 || value > 3) return fail(h, DSTIR_EINVAL, "p2g variant %lld not in 0..3", (long long)value);
         h->p2g_variant = (int)value;
         h->recorded = false;
         return DSTIR_OK;

@@ -45,7 +45,7 @@ __global__ void __launch_bounds__(256) bin_count_kernel(BinArgs b) {
         int base[3];
         float fx[3];
         if (locate(x, s.inv_dx, s.n, base, fx)) {
-            key = node_index(s, base[0], base[1], base[2]);
+            key = b.key_mode ? brick_key(s, base[0], base[1], base[2]) : node_index(s, base[0], base[1], base[2]);
         } else {
             key = b.G;  // overflow bin
             atomicOr(b.status, DSTIR_STATUS_OUT_OF_GRID);
@@ -436,6 +436,225 @@ __global__ void __launch_bounds__(256) g2p_adj_cell_kernel(AdjArgs a, const int*
                 red_add4(a.ga + row + k, acc[o][0], acc[o][1], acc[o][2], 0.f);
             }
         }
+}
+
+// ---------------------------------------------------------------------------
+// brick kernels: one CTA per brick of 4x4x4 cells, the brick's 6x6x6 stencil
+// nodes accumulated in shared memory and flushed with one vector atomic per
+// touched node.  Thread v handles particle j = v / 64 of cell c = v % 64, so
+// the 32 lanes of a warp belong to 32 different cells and, for a given stencil
+// offset, add into 32 different tile nodes (no same-address conflicts).
+// ---------------------------------------------------------------------------
+constexpr int TILE = 6;
+constexpr int TILE_NODES = TILE * TILE * TILE;
+
+__device__ __forceinline__ int tile_index(int li, int lj, int lk) { return (li * TILE + lj) * TILE + lk; }
+
+// shared prologue: brick header, the 65 cell starts, the largest cell count
+struct BrickCtx {
+    int cs[65];
+    int maxcnt;
+};
+
+__device__ __forceinline__ bool brick_prologue(const BrickInfo* bricks, const SceneDev* sc, const int* cell_start,
+                                               BrickInfo& br, SceneDev& s, BrickCtx& ctx) {
+    if (threadIdx.x == 0) {
+        br = bricks[blockIdx.x];
+        s = sc[br.scene];
+        ctx.maxcnt = 0;
+    }
+    __syncthreads();
+    if (threadIdx.x < 65) ctx.cs[threadIdx.x] = cell_start[br.key0 + threadIdx.x];
+    __syncthreads();
+    if (threadIdx.x < 64) atomicMax(&ctx.maxcnt, ctx.cs[threadIdx.x + 1] - ctx.cs[threadIdx.x]);
+    __syncthreads();
+    return ctx.cs[0] != ctx.cs[64];
+}
+
+template <bool SVDJ>
+__global__ void __launch_bounds__(256) p2g_brick_kernel(FwdArgs a, const BrickInfo* __restrict__ bricks,
+                                                        const int* __restrict__ cell_start,
+                                                        const int* __restrict__ perm, int n_bricks,
+                                                        long long nbins) {
+    __shared__ SceneDev s;
+    __shared__ BrickInfo br;
+    __shared__ BrickCtx ctx;
+    __shared__ float prm[4];
+    __shared__ int model;
+    __shared__ float tile[4][TILE_NODES];
+    if (blockIdx.x == (unsigned)n_bricks) {
+        // overflow bin: particles whose stencil left the grid get F[f+1], no scatter
+        int beg = cell_start[nbins], end = cell_start[nbins + 1];
+        for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+            long long p = perm[q];
+            int sc_i = 0;
+            while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
+            SceneDev s2 = a.sc[sc_i];
+            float pr[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) pr[i] = a.params[sc_i * 4 + i];
+            float x[3], m, mv[3], A[9];
+            p2g_particle<SVDJ>(a, s2, pr, a.models[sc_i], p, particle_kind(s2, p), x, m, mv, A);
+        }
+        return;
+    }
+    if (!brick_prologue(bricks, a.sc, cell_start, br, s, ctx)) return;
+    if (threadIdx.x < 4) prm[threadIdx.x] = a.params[br.scene * 4 + threadIdx.x];
+    if (threadIdx.x == 0) model = a.models[br.scene];
+    for (int i = threadIdx.x; i < 4 * TILE_NODES; i += blockDim.x) (&tile[0][0])[i] = 0.f;
+    __syncthreads();
+    const int oi = br.bi * 4, oj = br.bj * 4, ok = br.bk * 4;
+    const int nv = ctx.maxcnt * 64;
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+        const int c = v & 63, j = v >> 6;
+        const int q = ctx.cs[c] + j;
+        if (q >= ctx.cs[c + 1]) continue;
+        long long p = perm[q];
+        float x[3], m, mv[3], A[9];
+        p2g_particle<SVDJ>(a, s, prm, model, p, particle_kind(s, p), x, m, mv, A);
+        const int li = c >> 4, lj = (c >> 2) & 3, lk = c & 3;
+        float fx[3] = {x[0] * s.inv_dx - (float)(oi + li), x[1] * s.inv_dx - (float)(oj + lj),
+                       x[2] * s.inv_dx - (float)(ok + lk)};
+        float w[3][3];
+        bspline(fx, w);
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int jj = 0; jj < 3; ++jj) {
+                float wij = w[i][0] * w[jj][1];
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    float W = wij * w[k][2];
+                    float dp0 = ((float)i - fx[0]) * s.dx, dp1 = ((float)jj - fx[1]) * s.dx,
+                          dp2 = ((float)k - fx[2]) * s.dx;
+                    const int t = tile_index(li + i, lj + jj, lk + k);
+                    atomicAdd(&tile[0][t], W * (mv[0] + (A[0] * dp0 + A[1] * dp1 + A[2] * dp2)));
+                    atomicAdd(&tile[1][t], W * (mv[1] + (A[3] * dp0 + A[4] * dp1 + A[5] * dp2)));
+                    atomicAdd(&tile[2][t], W * (mv[2] + (A[6] * dp0 + A[7] * dp1 + A[8] * dp2)));
+                    atomicAdd(&tile[3][t], W * m);
+                }
+            }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
+        float g3 = tile[3][t], g0 = tile[0][t], g1 = tile[1][t], g2 = tile[2][t];
+        if (g3 == 0.f && g0 == 0.f && g1 == 0.f && g2 == 0.f) continue;
+        const int gi = oi + t / (TILE * TILE), gj = oj + (t / TILE) % TILE, gk = ok + t % TILE;
+        if (gi >= s.n || gj >= s.n || gk >= s.n) continue;
+        red_add4(a.pm + node_index(s, gi, gj, gk), g0, g1, g2, g3);
+    }
+}
+
+__global__ void __launch_bounds__(256) g2p_adj_brick_kernel(AdjArgs a, const BrickInfo* __restrict__ bricks,
+                                                            const int* __restrict__ cell_start,
+                                                            const int* __restrict__ perm, int n_bricks,
+                                                            long long nbins) {
+    __shared__ SceneDev s;
+    __shared__ BrickInfo br;
+    __shared__ BrickCtx ctx;
+    __shared__ float fb[3];
+    __shared__ float tile[3][TILE_NODES];
+    __shared__ float4 vt[TILE_NODES];
+    if (blockIdx.x == (unsigned)n_bricks) {
+        int beg = cell_start[nbins], end = cell_start[nbins + 1];
+        for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+            long long p = perm[q];
+            int sc_i = 0;
+            while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
+            if (particle_kind(a.sc[sc_i], p) == KIND_LIQUID) {
+                float ax[3];
+                load3(a.adj_next, a.stride, OX, p, ax);
+                store3(a.adj_cur, a.stride, OX, p, ax);
+            }
+        }
+        return;
+    }
+    if (!brick_prologue(bricks, a.sc, cell_start, br, s, ctx)) return;
+    if (threadIdx.x == 0) {
+        const float* d = a.dforce + br.scene * a.dforce_stride + (long long)a.fo * 3;
+        for (int c = 0; c < 3; ++c) fb[c] = d[c];
+    }
+    const int oi = br.bi * 4, oj = br.bj * 4, ok = br.bk * 4;
+    for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
+        tile[0][t] = tile[1][t] = tile[2][t] = 0.f;
+        const int gi = oi + t / (TILE * TILE), gj = oj + (t / TILE) % TILE, gk = ok + t % TILE;
+        vt[t] = (gi < s.n && gj < s.n && gk < s.n) ? __ldg(a.vo + node_index(s, gi, gj, gk))
+                                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __syncthreads();
+    const float c4 = 4.f * s.inv_dx;
+    const int nv = ctx.maxcnt * 64;
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+        const int c = v & 63, jv = v >> 6;
+        const int q = ctx.cs[c] + jv;
+        if (q >= ctx.cs[c + 1]) continue;
+        long long p = perm[q];
+        const int kind = particle_kind(s, p);
+        float x[3], vnb[3], xb[3], Cb[9];
+        load3(a.cur, a.stride, OX, p, x);
+        g2p_adj_particle_inputs(a, s, fb, p, kind, vnb, xb, Cb);
+        const int li = c >> 4, lj = (c >> 2) & 3, lk = c & 3;
+        float fx[3] = {x[0] * s.inv_dx - (float)(oi + li), x[1] * s.inv_dx - (float)(oj + lj),
+                       x[2] * s.inv_dx - (float)(ok + lk)};
+        float w[3][3], dw[3][3];
+        bspline_d(fx, w, dw);
+        float fxb[3] = {0.f, 0.f, 0.f};
+        const bool liquid = kind == KIND_LIQUID;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    const int t = tile_index(li + i, lj + j, lk + k);
+                    float W = w[i][0] * w[j][1] * w[k][2];
+                    float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
+                    float Cd0 = Cb[0] * d0 + Cb[1] * d1 + Cb[2] * d2;
+                    float Cd1 = Cb[3] * d0 + Cb[4] * d1 + Cb[5] * d2;
+                    float Cd2 = Cb[6] * d0 + Cb[7] * d1 + Cb[8] * d2;
+                    atomicAdd(&tile[0][t], W * (vnb[0] + c4 * Cd0));
+                    atomicAdd(&tile[1][t], W * (vnb[1] + c4 * Cd1));
+                    atomicAdd(&tile[2][t], W * (vnb[2] + c4 * Cd2));
+                    if (liquid) {
+                        float4 g = vt[t];
+                        float Wb = vnb[0] * g.x + vnb[1] * g.y + vnb[2] * g.z +
+                                   c4 * (g.x * Cd0 + g.y * Cd1 + g.z * Cd2);
+                        fxb[0] -= c4 * W * (Cb[0] * g.x + Cb[3] * g.y + Cb[6] * g.z);
+                        fxb[1] -= c4 * W * (Cb[1] * g.x + Cb[4] * g.y + Cb[7] * g.z);
+                        fxb[2] -= c4 * W * (Cb[2] * g.x + Cb[5] * g.y + Cb[8] * g.z);
+                        fxb[0] += Wb * dw[i][0] * w[j][1] * w[k][2];
+                        fxb[1] += Wb * w[i][0] * dw[j][1] * w[k][2];
+                        fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
+                    }
+                }
+        if (liquid) {
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) xb[cc] += s.inv_dx * fxb[cc];
+            store3(a.adj_cur, a.stride, OX, p, xb);
+        }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
+        float g0 = tile[0][t], g1 = tile[1][t], g2 = tile[2][t];
+        if (g0 == 0.f && g1 == 0.f && g2 == 0.f) continue;
+        const int gi = oi + t / (TILE * TILE), gj = oj + (t / TILE) % TILE, gk = ok + t % TILE;
+        if (gi >= s.n || gj >= s.n || gk >= s.n) continue;
+        red_add4(a.ga + node_index(s, gi, gj, gk), g0, g1, g2, 0.f);
+    }
+}
+
+void launch_p2g_brick(const FwdArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                      const int* perm, long long nbins, bool svdj, cudaStream_t st) {
+    if (n_bricks <= 0) return;
+    if (svdj)
+        p2g_brick_kernel<true><<<n_bricks + 1, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+    else
+        p2g_brick_kernel<false><<<n_bricks + 1, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+}
+
+void launch_g2p_adj_brick(const AdjArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                          const int* perm, long long nbins, cudaStream_t st) {
+    if (n_bricks > 0) g2p_adj_brick_kernel<<<n_bricks + 1, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
 }
 
 void launch_p2g_cell(const FwdArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,

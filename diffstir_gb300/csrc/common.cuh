@@ -23,9 +23,10 @@ enum Kind { KIND_LIQUID = 0, KIND_ROD = 1, KIND_CONTAINER = 2 };
 struct SceneDev {
     int n, bound, rod_mode, j_mode, container_wall, model;
     int n_liquid, n_rod, n_container;
-    int pad;
+    int nbr;          // bricks of 4x4x4 cells per axis, ceil(n/4)
     long long p0;     // first particle (global index) of the scene
     long long goff;   // first grid node of the scene
+    long long koff;   // first brick-major bin key of the scene (64 keys per brick)
     float dt, dx, inv_dx, gravity, bulk, alpha;  // alpha = -dt*V_p*4*inv_dx^2 (:150)
     float m_liq, m_rod, m_cont, force_scale;
     float ccx, ccz, cr2;  // container axis and squared projection radius (:205-207)
@@ -91,6 +92,21 @@ __device__ __forceinline__ void bspline_d(const float fx[3], float w[3][3], floa
 __device__ __forceinline__ long long node_index(const SceneDev& s, int i, int j, int k) {
     return s.goff + ((long long)i * s.n + j) * s.n + k;
 }
+
+// Brick-major bin key of cell (i,j,k): bricks of 4x4x4 cells in (i,j,k)-major
+// order, then the cell inside its brick, so that the 64 cells of a brick own
+// one contiguous range of the sorted particle list.
+__device__ __forceinline__ long long brick_key(const SceneDev& s, int i, int j, int k) {
+    long long br = ((long long)(i >> 2) * s.nbr + (j >> 2)) * s.nbr + (k >> 2);
+    return s.koff + br * 64 + (((i & 3) * 4 + (j & 3)) * 4 + (k & 3));
+}
+
+// One CTA of a brick kernel: the brick's first cell and its first bin key.
+struct BrickInfo {
+    int scene, bi, bj, bk;
+    long long key0;
+    long long pad;
+};
 
 __device__ __forceinline__ void matmul3(const float* A, const float* B, float* o) {
 #pragma unroll

@@ -70,13 +70,14 @@ struct BinArgs {
     int* cell_start;         // [G+2] exclusive prefix of the counts
     int* perm;               // [N] particle indices sorted by bin
     int* bsum;               // scan scratch, bin_scan_blocks(G) entries
-    long long G;
+    long long G;             // number of bins (the overflow bin is G)
     unsigned* status;
+    int key_mode;            // 0: bin = grid node of the stencil base; 1: brick-major key
 };
 
 // p2g variants: scalar atomics per particle, vector atomics per particle,
 // binned one-thread-per-cell accumulation
-enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_CELL = 2 };
+enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_CELL = 2, P2G_BRICK = 3 };
 
 void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st);
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st);
@@ -92,6 +93,11 @@ void launch_p2g_cell(const FwdArgs& a, const int* cell_start, const int* perm, i
                      long long G, bool svdj, cudaStream_t st);
 void launch_g2p_adj_cell(const AdjArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
                          long long G, cudaStream_t st);
+
+void launch_p2g_brick(const FwdArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                      const int* perm, long long nbins, bool svdj, cudaStream_t st);
+void launch_g2p_adj_brick(const AdjArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                          const int* perm, long long nbins, cudaStream_t st);
 
 void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
                        long long stride, long long n, cudaStream_t s);

@@ -138,9 +138,14 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams,
  * gradient_descent_module.py:51-54.) */
 int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
 
-/* Tuning knobs: "p2g" (0 plain scalar atomics, 1 vector atomics, 2 binned
- * shared-memory tiles), "block" (threads per block), "graph" (1: capture each
- * checkpoint segment as a CUDA graph), "tile" (tile cells per CTA). */
+/* Tuning knobs: "p2g" (0 scalar atomics per particle, 1 vector atomics per
+ * particle, 2 cell-binned one-thread-per-cell accumulation, 3 brick-binned
+ * shared-memory tiles with one CTA per 4x4x4-cell brick; 2 and 3 also select
+ * the matching G2P-adjoint scatter), "block" / "gblock" (threads per particle /
+ * grid block: 64, 128 or 256), "graph" (1: replay each rollout and each
+ * reverse pass as a cached CUDA graph), "profile" (1: time every launch with
+ * CUDA events; totals via dstir_get_option "prof_ns:<kernel>" /
+ * "prof_count:<kernel>"), "launches" (reset the launch counter). */
 int dstir_set_option(DstirHandle* h, const char* key, int64_t value);
 int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value);
 

@@ -64,8 +64,8 @@ def fixture_scene(name, model):
                  d['operator_trajectory'], d['m%d_params' % model]), d
 
 
-VARIANTS = [{'p2g': 1}, {'p2g': 2}, {'p2g': 2, 'graph': 1}]
-VARIANT_IDS = ['vec-atomics', 'binned', 'binned-graph']
+VARIANTS = [{'p2g': 1}, {'p2g': 2}, {'p2g': 3}, {'p2g': 3, 'graph': 1}]
+VARIANT_IDS = ['vec-atomics', 'cell-binned', 'brick-tiled', 'brick-graph']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
@@ -136,7 +136,8 @@ def test_p2g_variants_agree():
     sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=5))
     wts = np.random.default_rng(4).normal(size=(T, 3))
     f0, g0, _, _ = gpu_force_and_grad(sc, T, wts, options={'p2g': 0})
-    for opts in ({'p2g': 1}, {'p2g': 2}, {'p2g': 2, 'block': 128, 'gblock': 128}, {'p2g': 1, 'graph': 1}):
+    for opts in ({'p2g': 1}, {'p2g': 2}, {'p2g': 2, 'block': 128, 'gblock': 128}, {'p2g': 1, 'graph': 1},
+                 {'p2g': 3}, {'p2g': 3, 'block': 64, 'gblock': 128}):
         f1, g1, _, _ = gpu_force_and_grad(sc, T, wts, options=opts)
         assert rel(f1, f0) < 1e-5, opts
         assert rel(g1, g0) < 1e-4, opts
@@ -174,7 +175,7 @@ def test_batched_equals_single():
                                  (1, 0.42, (2.0, 0.1, 0.6, 0.8), S.MODEL_CARREAU),
                                  (2, 0.22, (0.9, 0.4, 0.8, 0.0), S.MODEL_HB))]
     wts = np.random.default_rng(5).normal(size=(len(scenes), T, 3))
-    for opts in ({'p2g': 1}, {'p2g': 2, 'graph': 1}):
+    for opts in ({'p2g': 1}, {'p2g': 2, 'graph': 1}, {'p2g': 3}):
         sim = Simulator(scenes, max_steps=T, options=opts)
         force = sim.forward(T, ckpt_every=6, record=True).cpu().numpy()
         dp = sim.backward(torch.as_tensor(wts, dtype=torch.float32, device='cuda')).cpu().numpy()
