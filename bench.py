@@ -64,6 +64,8 @@ def parse():
     ap.add_argument('--block', type=int, default=None)
     ap.add_argument('--gblock', type=int, default=None)
     ap.add_argument('--autotune', type=int, default=1, help='1: launch options from the autotuner (cached)')
+    ap.add_argument('--brick-scatter', type=int, default=None, help='brick P2G scatter: 0 atom, 1 red.shared, 2 global')
+    ap.add_argument('--brick-gather', type=int, default=None)
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')
@@ -234,11 +236,12 @@ def run_ours(args):
     scenes, T, ckpt = build_workload(args, rank)
     sc = scenes[0]
     opts = {}
-    explicit = any(getattr(args, k) is not None for k in ('p2g', 'graph', 'block', 'gblock'))
+    keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather')
+    explicit = any(getattr(args, k) is not None for k in keys)
     if args.autotune and not explicit:
         from diffstir_gb300 import autotune
         opts = autotune.autotune(scenes)
-    for k in ('p2g', 'graph', 'block', 'gblock'):
+    for k in keys:
         if getattr(args, k) is not None:
             opts[k] = getattr(args, k)
     sim = Simulator(scenes, max_steps=T, options=opts)
@@ -278,7 +281,6 @@ def run_ours(args):
 
     clocks = ClockSampler(local)
     clocks.start()
-    sim.set_option('profile', 1)
     sim.set_option('launches', 0)
     stream = torch.cuda.current_stream()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -292,9 +294,19 @@ def run_ours(args):
     barrier()
     ms = e0.elapsed_time(e1) / args.steps
     launches = sim.get_option('launches')
+    clk = clocks.stop()
+    # per-kernel CUDA-event times: one more identical step with every launch
+    # bracketed by events on the launching stream (kept out of the timed steps,
+    # whose value the event records would perturb for small scenes; graph
+    # replay is switched off for this pass so that each launch is visible)
+    graph_was = sim.get_option('graph')
+    sim.set_option('graph', 0)
+    sim.set_option('profile', 1)
+    grad_eval(params)
+    torch.cuda.synchronize()
     prof = {k: (sim.get_option('prof_ns:' + k) / 1e6, sim.get_option('prof_count:' + k)) for k in KERNELS}
     sim.set_option('profile', 0)
-    clk = clocks.stop()
+    sim.set_option('graph', graph_was)
     if world > 1:
         import torch.distributed as dist
         t = torch.tensor([ms], device=dev)
@@ -391,7 +403,7 @@ def run_ours(args):
         'cpu_baseline': cpu,
         'e2e': e2e,
         'gpu_launches': int(launches),
-        'options': {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock')},
+        'options': {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather')},
         'clocks': clk,
         'status_flags': int(st),
     }

@@ -1,0 +1,172 @@
+// Per-particle pieces of the P2G adjoint (the reverse of p2g,
+// simulation_functions.py:104-196, and of compute_F_tmp :39-42) shared by the
+// per-particle kernel (kernels.cu) and the brick kernel (binning.cu).  The work
+// is split so that few values stay live across the 27-node gather:
+//   p2g_adj_affine   recompute the particle's affine momentum A and m v'
+//   (caller)         gather the P/M adjoint over the stencil -> Ab, vvb, fxb
+//   p2g_adj_finish   reload C and F; stress, bulk, viscosity and F_tmp
+//                    adjoints; write the state adjoint; parameter partials
+#pragma once
+
+#include "common.cuh"
+#include "device_util.cuh"
+#include "internal.h"
+#include "svd.cuh"
+
+namespace dstir {
+
+template <bool SVDJ>
+__device__ __forceinline__ void p2g_adj_affine(const float* cur, long long stride, const SceneDev& s,
+                                               const float* prm, int model, long long p, int kind, float& m,
+                                               float mv[3], float A[9]) {
+    float v[3], C[9];
+    load3(cur, stride, OV, p, v);
+    load9(cur, stride, OC, p, C);
+    if (kind == KIND_LIQUID) {
+        float F[9];
+        load9(cur, stride, OF, p, F);
+        LiquidP2G q;
+        liquid_p2g<SVDJ>(s, model, prm, v, C, F, q);
+        m = s.m_liq;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = q.A[i];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) mv[c] = m * q.vv[c];
+    } else {
+        m = (kind == KIND_ROD) ? s.m_rod : s.m_cont;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) A[i] = m * C[i];
+#pragma unroll
+        for (int c = 0; c < 3; ++c) mv[c] = m * v[c];
+    }
+}
+
+// Gather contribution of one stencil node (weight W, derivative weights
+// dWx/dWy/dWz in fx, dpos dp, node adjoint gb) to Ab, vvb (not yet times m)
+// and fxb.
+__device__ __forceinline__ void p2g_adj_node(float W, float dWx, float dWy, float dWz, const float dp[3], float4 gb,
+                                             float m, const float mv[3], const float A[9], float dx, bool liquid,
+                                             float Ab[9], float vvb[3], float fxb[3]) {
+    float gbv[3] = {gb.x, gb.y, gb.z};
+    float Wb = gb.w * m;
+#pragma unroll
+    for (int aa = 0; aa < 3; ++aa) {
+        float ad = A[aa * 3 + 0] * dp[0] + A[aa * 3 + 1] * dp[1] + A[aa * 3 + 2] * dp[2];
+        Wb += gbv[aa] * (mv[aa] + ad);
+        vvb[aa] += W * gbv[aa];
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) Ab[aa * 3 + bb] += W * gbv[aa] * dp[bb];
+    }
+    if (liquid) {
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb)
+            fxb[bb] -= W * dx * (A[0 * 3 + bb] * gbv[0] + A[1 * 3 + bb] * gbv[1] + A[2 * 3 + bb] * gbv[2]);
+        fxb[0] += Wb * dWx;
+        fxb[1] += Wb * dWy;
+        fxb[2] += Wb * dWz;
+    }
+}
+
+template <bool SVDJ>
+__device__ __forceinline__ void p2g_adj_finish(const AdjArgs& a, const SceneDev& s, const float* prm, int model,
+                                               long long p, int kind, float m, const float Ab[9], float vvb[3],
+                                               const float fxb[3], float pg[4]) {
+#pragma unroll
+    for (int c = 0; c < 3; ++c) vvb[c] *= m;
+    if (kind != KIND_LIQUID) {
+        float Cb[9], z[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) {
+            Cb[i] = m * Ab[i];
+            z[i] = 0.f;
+        }
+        store3(a.adj_cur, a.stride, OX, p, z);
+        store3(a.adj_cur, a.stride, OV, p, z);
+        store9(a.adj_cur, a.stride, OC, p, Cb);
+        store9(a.adj_cur, a.stride, OF, p, z);
+        return;
+    }
+    float xb[3];
+    load3(a.adj_cur, a.stride, OX, p, xb);  // G2P part, written by the G2P adjoint
+#pragma unroll
+    for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
+    store3(a.adj_cur, a.stride, OX, p, xb);
+    store3(a.adj_cur, a.stride, OV, p, vvb);
+    float C[9], F[9], IC[9], Ft[9];
+    load9(a.cur, a.stride, OC, p, C);
+    load9(a.cur, a.stride, OF, p, F);
+#pragma unroll
+    for (int i = 0; i < 9; ++i) IC[i] = s.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
+    matmul3(IC, F, Ft);
+    float U[9], sg[3], Vm[9], J;
+    if (SVDJ && s.j_mode == DSTIR_J_SVD) {
+        svd3(Ft, U, sg, Vm);
+        J = sg[0] * sg[1] * sg[2];
+    } else {
+        J = det3(Ft);
+    }
+    float nrm2 = 0.f;
+#pragma unroll
+    for (int i = 0; i < 9; ++i) nrm2 += C[i] * C[i];
+    float nrm = sqrtf(nrm2);
+    Visc vs = viscosity<true>(model, prm, nrm + 1e-6f);
+    float Cb[9], sigb[9];
+#pragma unroll
+    for (int i = 0; i < 9; ++i) {
+        Cb[i] = m * Ab[i];
+        sigb[i] = s.alpha * Ab[i];
+    }
+    float etab = 0.f;
+#pragma unroll
+    for (int aa = 0; aa < 3; ++aa)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) {
+            float Dab = 0.5f * (C[aa * 3 + bb] + C[bb * 3 + aa]);
+            etab += sigb[aa * 3 + bb] * Dab;
+            Cb[aa * 3 + bb] += vs.eta * 0.5f * (sigb[aa * 3 + bb] + sigb[bb * 3 + aa]);
+        }
+    float trb = sigb[0] + sigb[4] + sigb[8];
+    float Jb = trb * (s.bulk / 2.f) * (2.f * J - 1.f);
+    float Ftb[9];
+    load9(a.adj_next, a.stride, OF, p, Ftb);  // F[f+1] = F_tmp
+    if (SVDJ && s.j_mode == DSTIR_J_SVD) {
+        float gS[3] = {Jb * sg[1] * sg[2], Jb * sg[0] * sg[2], Jb * sg[0] * sg[1]};
+        float z[9], gA[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) z[i] = 0.f;
+        svd3_backward(z, gS, z, U, sg, Vm, gA);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Ftb[i] += gA[i];
+    } else {
+        float cf[9];
+        cof3(Ft, cf);
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Ftb[i] += Jb * cf[i];
+    }
+    float gammab = etab * vs.deta_dgamma;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) pg[i] += etab * vs.dp[i];
+    if (nrm > 0.f) {
+        float inv = gammab / nrm;
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Cb[i] += inv * C[i];
+    }
+    float Fb[9];
+#pragma unroll
+    for (int aa = 0; aa < 3; ++aa)
+#pragma unroll
+        for (int bb = 0; bb < 3; ++bb) {
+            float sF = 0.f, sC = 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                sF += IC[c * 3 + aa] * Ftb[c * 3 + bb];
+                sC += Ftb[aa * 3 + c] * F[bb * 3 + c];
+            }
+            Fb[aa * 3 + bb] = sF;
+            Cb[aa * 3 + bb] += s.dt * sC;
+        }
+    store9(a.adj_cur, a.stride, OC, p, Cb);
+    store9(a.adj_cur, a.stride, OF, p, Fb);
+}
+
+}  // namespace dstir

@@ -105,6 +105,8 @@ struct DstirHandle {
     std::vector<SceneDev> sc_h;
     long long N = 0, stride = 0, G = 0;
     int block = 256, gblock = 256, p2g_variant = P2G_VEC, use_graph = 0;
+    int brick_gather = 1;   // with P2G_BRICK: G2P and the P2G adjoint also gather from brick tiles
+    int brick_scatter = 1;  // with P2G_BRICK: 0 shared atomics, 1 shared red, 2 direct global atomics
     std::vector<BlockInfo> blk_h;
     std::vector<GridBlock> gblk_h;
     SceneDev* sc = nullptr;
@@ -251,7 +253,9 @@ int build_tables(DstirHandle* h) {
     CUDA_TRY(h, cudaMemcpy(h->blk, h->blk_h.data(), h->blk_h.size() * sizeof(BlockInfo), cudaMemcpyHostToDevice));
     CUDA_TRY(h, cudaMemcpy(h->gblk, h->gblk_h.data(), h->gblk_h.size() * sizeof(GridBlock),
                            cudaMemcpyHostToDevice));
-    long long pl = std::max<long long>(std::max(h->n_blocks, h->n_gblocks), 1);
+    // partial sums are indexed by the CTA of any reducing kernel: particle
+    // blocks, grid blocks, or bricks (+ the overflow CTAs)
+    long long pl = std::max<long long>(std::max(std::max(h->n_blocks, h->n_gblocks), h->n_bricks + 64), 1);
     if (pl > h->partial_len) {
         if ((rc = dalloc(h, &h->partial, (size_t)pl * 4, "partial sums"))) return rc;
         h->partial_len = pl;
@@ -354,7 +358,8 @@ void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot
         timed(h, K_BIN, st, [&] { launch_bin(b, h->n_blocks, h->block, st); });
         if (brick)
             timed(h, K_P2G, st, [&] {
-                launch_p2g_brick(a, h->bricks, h->n_bricks, b.cell_start, b.perm, b.G, h->any_svd, st);
+                launch_p2g_brick(a, h->bricks, h->n_bricks, b.cell_start, b.perm, b.G, h->any_svd, h->brick_scatter,
+                                 st);
             });
         else
             timed(h, K_P2G, st, [&] {
@@ -364,14 +369,20 @@ void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot
         timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st); });
     }
     timed(h, K_GRID, st, [&] { launch_grid(a, h->n_gblocks, h->gblock, st); });
-    timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st); });
+    if (h->p2g_variant == P2G_BRICK && h->brick_gather)
+        timed(h, K_G2P, st, [&] {
+            launch_g2p_brick(a, h->bricks, h->n_bricks, slot_cell_start(h, bin_slot), slot_perm(h, bin_slot),
+                             h->nbins_brick, st);
+        });
+    else
+        timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st); });
 }
 
 void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st, int bin_slot = 0) {
     if (h->p2g_variant == P2G_BRICK) {
         timed(h, K_G2P_ADJ, st, [&] {
             launch_g2p_adj_brick(a, h->bricks, h->n_bricks, slot_cell_start(h, bin_slot), slot_perm(h, bin_slot),
-                                 h->nbins_brick, st);
+                                 h->nbins_brick, h->brick_scatter, st);
         });
     } else if (h->p2g_variant == P2G_CELL) {
         timed(h, K_G2P_ADJ, st, [&] {
@@ -383,7 +394,13 @@ void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st, int bin_
         timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st); });
     }
     timed(h, K_GRID_ADJ, st, [&] { launch_grid_adj(a, h->n_gblocks, h->gblock, st); });
-    timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st); });
+    if (h->p2g_variant == P2G_BRICK && h->brick_gather)
+        timed(h, K_P2G_ADJ, st, [&] {
+            launch_p2g_adj_brick(a, h->bricks, h->n_bricks, slot_cell_start(h, bin_slot), slot_perm(h, bin_slot),
+                                 h->nbins_brick, h->any_svd, st);
+        });
+    else
+        timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st); });
 }
 
 }  // namespace
@@ -437,7 +454,8 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
                     b.bj = bj;
                     b.bk = bk;
                     b.key0 = sd.koff + (((long long)bi * sd.nbr + bj) * sd.nbr + bk) * 64;
-                    b.pad = 0;
+                    b.idx = (int)(((long long)bi * sd.nbr + bj) * sd.nbr + bk);
+                    b.count = sd.nbr * sd.nbr * sd.nbr;
                     h->bricks_h.push_back(b);
                 }
         h->nbins_brick += 64LL * sd.nbr * sd.nbr * sd.nbr;
@@ -839,6 +857,19 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         h->use_graph = value ? 1 : 0;
         return DSTIR_OK;
     }
+    if (!strcmp(key, "brick_scatter")) {
+        if (value < 0 || value > 2) return fail(h, DSTIR_EINVAL, "brick_scatter %lld not in 0..2", (long long)value);
+        h->brick_scatter = (int)value;
+        h->recorded = false;
+        ++h->epoch;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "brick_gather")) {
+        h->brick_gather = value ? 1 : 0;
+        h->recorded = false;
+        ++h->epoch;
+        return DSTIR_OK;
+    }
     if (!strcmp(key, "profile")) {  // 1: time every launch with CUDA events; resets the totals
         h->prof.reset();
         h->prof.on = value != 0;
@@ -857,6 +888,8 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "block")) *value = h->block;
     else if (!strcmp(key, "gblock")) *value = h->gblock;
     else if (!strcmp(key, "graph")) *value = h->use_graph;
+    else if (!strcmp(key, "brick_gather")) *value = h->brick_gather;
+    else if (!strcmp(key, "brick_scatter")) *value = h->brick_scatter;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

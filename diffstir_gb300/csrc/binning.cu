@@ -18,12 +18,15 @@
 #include "common.cuh"
 #include "device_util.cuh"
 #include "internal.h"
+#include "adjoint.cuh"
 
 namespace dstir {
 
 constexpr int SCAN_THREADS = 256;
 constexpr int SCAN_PER_THREAD = 16;
 constexpr int SCAN_CHUNK = SCAN_THREADS * SCAN_PER_THREAD;
+// CTAs after the last brick / grid block that share the overflow bin
+constexpr int OVERFLOW_CTAS = 64;
 
 // ---------------------------------------------------------------------------
 // counting sort by cell
@@ -237,7 +240,7 @@ __global__ void __launch_bounds__(256) p2g_cell_kernel(FwdArgs a, const int* __r
     __shared__ GridBlock gb;
     __shared__ float prm[4];
     __shared__ int model;
-    const bool overflow = blockIdx.x == (unsigned)n_gblocks;
+    const bool overflow = blockIdx.x >= (unsigned)n_gblocks;
     if (threadIdx.x == 0) {
         gb = a.gblk[overflow ? 0 : blockIdx.x];
         s = a.sc[gb.scene];
@@ -246,7 +249,8 @@ __global__ void __launch_bounds__(256) p2g_cell_kernel(FwdArgs a, const int* __r
     if (overflow) {
         // particles outside the grid: F[f+1] only, no scatter (status was raised when binning)
         int beg = cell_start[G], end = cell_start[G + 1];
-        for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+        const unsigned first = blockIdx.x - (unsigned)(gridDim.x - OVERFLOW_CTAS);
+        for (int q = beg + first * blockDim.x + threadIdx.x; q < end; q += OVERFLOW_CTAS * blockDim.x) {
             long long p = perm[q];
             int sc_i = 0;
             while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
@@ -345,11 +349,12 @@ __global__ void __launch_bounds__(256) g2p_adj_cell_kernel(AdjArgs a, const int*
     __shared__ SceneDev s;
     __shared__ GridBlock gb;
     __shared__ float fb[3];
-    const bool overflow = blockIdx.x == (unsigned)n_gblocks;
+    const bool overflow = blockIdx.x >= (unsigned)n_gblocks;
     if (overflow) {
         // particles outside the grid: only x[f+1] = x[f] + dt v[f+1] carries an adjoint
         int beg = cell_start[G], end = cell_start[G + 1];
-        for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+        const unsigned first = blockIdx.x - (unsigned)(gridDim.x - OVERFLOW_CTAS);
+        for (int q = beg + first * blockDim.x + threadIdx.x; q < end; q += OVERFLOW_CTAS * blockDim.x) {
             long long p = perm[q];
             int sc_i = 0;
             while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
@@ -448,7 +453,29 @@ __global__ void __launch_bounds__(256) g2p_adj_cell_kernel(AdjArgs a, const int*
 constexpr int TILE = 6;
 constexpr int TILE_NODES = TILE * TILE * TILE;
 
+
 __device__ __forceinline__ int tile_index(int li, int lj, int lk) { return (li * TILE + lj) * TILE + lk; }
+
+// How a brick kernel adds one stencil contribution:
+//   SCATTER_ATOM    shared tile, atomicAdd
+//   SCATTER_RED     shared tile, no-return red.shared.add.f32
+//   SCATTER_GLOBAL  straight to the global grid with one vector atomic per node
+//                   (lanes of a warp hit 32 different nodes, so L2 never
+//                   serialises same-address updates inside one request)
+enum { SCATTER_ATOM = 0, SCATTER_RED = 1, SCATTER_GLOBAL = 2 };
+
+__device__ __forceinline__ void shared_red_add(float* p, float v) {
+    unsigned a = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("red.shared.add.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+
+template <int MODE>
+__device__ __forceinline__ void tile_add(float* p, float v) {
+    if (MODE == SCATTER_RED)
+        shared_red_add(p, v);
+    else
+        atomicAdd(p, v);
+}
 
 // shared prologue: brick header, the 65 cell starts, the largest cell count
 struct BrickCtx {
@@ -471,7 +498,7 @@ __device__ __forceinline__ bool brick_prologue(const BrickInfo* bricks, const Sc
     return ctx.cs[0] != ctx.cs[64];
 }
 
-template <bool SVDJ>
+template <bool SVDJ, int MODE>
 __global__ void __launch_bounds__(256) p2g_brick_kernel(FwdArgs a, const BrickInfo* __restrict__ bricks,
                                                         const int* __restrict__ cell_start,
                                                         const int* __restrict__ perm, int n_bricks,
@@ -482,10 +509,11 @@ __global__ void __launch_bounds__(256) p2g_brick_kernel(FwdArgs a, const BrickIn
     __shared__ float prm[4];
     __shared__ int model;
     __shared__ float tile[4][TILE_NODES];
-    if (blockIdx.x == (unsigned)n_bricks) {
+    if (blockIdx.x >= (unsigned)n_bricks) {
         // overflow bin: particles whose stencil left the grid get F[f+1], no scatter
         int beg = cell_start[nbins], end = cell_start[nbins + 1];
-        for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+        const unsigned first = blockIdx.x - (unsigned)(gridDim.x - OVERFLOW_CTAS);
+        for (int q = beg + first * blockDim.x + threadIdx.x; q < end; q += OVERFLOW_CTAS * blockDim.x) {
             long long p = perm[q];
             int sc_i = 0;
             while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
@@ -527,14 +555,22 @@ __global__ void __launch_bounds__(256) p2g_brick_kernel(FwdArgs a, const BrickIn
                     float W = wij * w[k][2];
                     float dp0 = ((float)i - fx[0]) * s.dx, dp1 = ((float)jj - fx[1]) * s.dx,
                           dp2 = ((float)k - fx[2]) * s.dx;
-                    const int t = tile_index(li + i, lj + jj, lk + k);
-                    atomicAdd(&tile[0][t], W * (mv[0] + (A[0] * dp0 + A[1] * dp1 + A[2] * dp2)));
-                    atomicAdd(&tile[1][t], W * (mv[1] + (A[3] * dp0 + A[4] * dp1 + A[5] * dp2)));
-                    atomicAdd(&tile[2][t], W * (mv[2] + (A[6] * dp0 + A[7] * dp1 + A[8] * dp2)));
-                    atomicAdd(&tile[3][t], W * m);
+                    const float g0 = W * (mv[0] + (A[0] * dp0 + A[1] * dp1 + A[2] * dp2));
+                    const float g1 = W * (mv[1] + (A[3] * dp0 + A[4] * dp1 + A[5] * dp2));
+                    const float g2 = W * (mv[2] + (A[6] * dp0 + A[7] * dp1 + A[8] * dp2));
+                    if (MODE == SCATTER_GLOBAL) {
+                        red_add4(a.pm + node_index(s, oi + li + i, oj + lj + jj, ok + lk + k), g0, g1, g2, W * m);
+                    } else {
+                        const int t = tile_index(li + i, lj + jj, lk + k);
+                        tile_add<MODE>(&tile[0][t], g0);
+                        tile_add<MODE>(&tile[1][t], g1);
+                        tile_add<MODE>(&tile[2][t], g2);
+                        tile_add<MODE>(&tile[3][t], W * m);
+                    }
                 }
             }
     }
+    if (MODE == SCATTER_GLOBAL) return;
     __syncthreads();
     for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
         float g3 = tile[3][t], g0 = tile[0][t], g1 = tile[1][t], g2 = tile[2][t];
@@ -545,6 +581,7 @@ __global__ void __launch_bounds__(256) p2g_brick_kernel(FwdArgs a, const BrickIn
     }
 }
 
+template <int MODE>
 __global__ void __launch_bounds__(256) g2p_adj_brick_kernel(AdjArgs a, const BrickInfo* __restrict__ bricks,
                                                             const int* __restrict__ cell_start,
                                                             const int* __restrict__ perm, int n_bricks,
@@ -555,9 +592,10 @@ __global__ void __launch_bounds__(256) g2p_adj_brick_kernel(AdjArgs a, const Bri
     __shared__ float fb[3];
     __shared__ float tile[3][TILE_NODES];
     __shared__ float4 vt[TILE_NODES];
-    if (blockIdx.x == (unsigned)n_bricks) {
+    if (blockIdx.x >= (unsigned)n_bricks) {
         int beg = cell_start[nbins], end = cell_start[nbins + 1];
-        for (int q = beg + threadIdx.x; q < end; q += blockDim.x) {
+        const unsigned first = blockIdx.x - (unsigned)(gridDim.x - OVERFLOW_CTAS);
+        for (int q = beg + first * blockDim.x + threadIdx.x; q < end; q += OVERFLOW_CTAS * blockDim.x) {
             long long p = perm[q];
             int sc_i = 0;
             while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
@@ -612,9 +650,14 @@ __global__ void __launch_bounds__(256) g2p_adj_brick_kernel(AdjArgs a, const Bri
                     float Cd0 = Cb[0] * d0 + Cb[1] * d1 + Cb[2] * d2;
                     float Cd1 = Cb[3] * d0 + Cb[4] * d1 + Cb[5] * d2;
                     float Cd2 = Cb[6] * d0 + Cb[7] * d1 + Cb[8] * d2;
-                    atomicAdd(&tile[0][t], W * (vnb[0] + c4 * Cd0));
-                    atomicAdd(&tile[1][t], W * (vnb[1] + c4 * Cd1));
-                    atomicAdd(&tile[2][t], W * (vnb[2] + c4 * Cd2));
+                    if (MODE == SCATTER_GLOBAL) {
+                        red_add4(a.ga + node_index(s, oi + li + i, oj + lj + j, ok + lk + k), W * (vnb[0] + c4 * Cd0),
+                                 W * (vnb[1] + c4 * Cd1), W * (vnb[2] + c4 * Cd2), 0.f);
+                    } else {
+                        tile_add<MODE>(&tile[0][t], W * (vnb[0] + c4 * Cd0));
+                        tile_add<MODE>(&tile[1][t], W * (vnb[1] + c4 * Cd1));
+                        tile_add<MODE>(&tile[2][t], W * (vnb[2] + c4 * Cd2));
+                    }
                     if (liquid) {
                         float4 g = vt[t];
                         float Wb = vnb[0] * g.x + vnb[1] * g.y + vnb[2] * g.z +
@@ -633,6 +676,7 @@ __global__ void __launch_bounds__(256) g2p_adj_brick_kernel(AdjArgs a, const Bri
             store3(a.adj_cur, a.stride, OX, p, xb);
         }
     }
+    if (MODE == SCATTER_GLOBAL) return;
     __syncthreads();
     for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
         float g0 = tile[0][t], g1 = tile[1][t], g2 = tile[2][t];
@@ -643,32 +687,279 @@ __global__ void __launch_bounds__(256) g2p_adj_brick_kernel(AdjArgs a, const Bri
     }
 }
 
-void launch_p2g_brick(const FwdArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
-                      const int* perm, long long nbins, bool svdj, cudaStream_t st) {
+// G2P from a shared-memory tile of the brick's 6x6x6 velocity nodes.  Every
+// brick CTA of a scene joins the deterministic rod-force reduction
+// (particle rod mode), empty bricks included.
+__global__ void __launch_bounds__(256) g2p_brick_kernel(FwdArgs a, const BrickInfo* __restrict__ bricks,
+                                                        const int* __restrict__ cell_start,
+                                                        const int* __restrict__ perm, int n_bricks,
+                                                        long long nbins) {
+    __shared__ SceneDev s;
+    __shared__ BrickInfo br;
+    __shared__ BrickCtx ctx;
+    __shared__ float sh[32][4];
+    __shared__ float tv[3];
+    __shared__ float4 vt[TILE_NODES];
+    if (blockIdx.x >= (unsigned)n_bricks) {
+        // overflow bin: no gather (v and C of the G2P are zero), as g2p_kernel does
+        int beg = cell_start[nbins], end = cell_start[nbins + 1];
+        const unsigned first = blockIdx.x - (unsigned)(gridDim.x - OVERFLOW_CTAS);
+        for (int q = beg + first * blockDim.x + threadIdx.x; q < end; q += OVERFLOW_CTAS * blockDim.x) {
+            long long p = perm[q];
+            int sc_i = 0;
+            while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
+            const SceneDev& s2 = a.sc[sc_i];
+            const int kind = particle_kind(s2, p);
+            const float* t0 = a.traj + ((long long)sc_i * a.traj_len + a.f) * 3;
+            float x[3], z[9], outv[3], nx[3];
+            load3(a.cur, a.stride, OX, p, x);
+#pragma unroll
+            for (int c = 0; c < 9; ++c) z[c] = 0.f;
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                float tvc = (t0[3 + c] - t0[c]) / s2.dt;
+                outv[c] = (kind == KIND_ROD) ? tvc : 0.f;
+                nx[c] = (kind == KIND_ROD) ? x[c] + tvc * s2.dt : x[c];
+            }
+            store9(a.next, a.stride, OC, p, z);
+            store3(a.next, a.stride, OV, p, outv);
+            store3(a.next, a.stride, OX, p, nx);
+        }
+        return;
+    }
+    brick_prologue(bricks, a.sc, cell_start, br, s, ctx);
+    const int oi = br.bi * 4, oj = br.bj * 4, ok = br.bk * 4;
+    if (threadIdx.x == 0) {
+        const float* t0 = a.traj + ((long long)br.scene * a.traj_len + a.f) * 3;
+        for (int c = 0; c < 3; ++c) tv[c] = (t0[3 + c] - t0[c]) / s.dt;
+    }
+    if (ctx.cs[0] != ctx.cs[64])
+        for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
+            const int gi = oi + t / (TILE * TILE), gj = oj + (t / TILE) % TILE, gk = ok + t % TILE;
+            vt[t] = (gi < s.n && gj < s.n && gk < s.n) ? __ldg(a.vo + node_index(s, gi, gj, gk))
+                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    __syncthreads();
+    float dv[3] = {0.f, 0.f, 0.f};
+    bool any_nan = false;
+    const int nv = ctx.maxcnt * 64;
+    const float c4 = 4.f * s.inv_dx;
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+        const int c = v & 63, jv = v >> 6;
+        const int q = ctx.cs[c] + jv;
+        if (q >= ctx.cs[c + 1]) continue;
+        long long p = perm[q];
+        const int kind = particle_kind(s, p);
+        float x[3];
+        load3(a.cur, a.stride, OX, p, x);
+        const int li = c >> 4, lj = (c >> 2) & 3, lk = c & 3;
+        float fx[3] = {x[0] * s.inv_dx - (float)(oi + li), x[1] * s.inv_dx - (float)(oj + lj),
+                       x[2] * s.inv_dx - (float)(ok + lk)};
+        float w[3][3];
+        bspline(fx, w);
+        float nv3[3] = {0.f, 0.f, 0.f}, nC[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) nC[i] = 0.f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    float4 g = vt[tile_index(li + i, lj + j, lk + k)];
+                    float W = w[i][0] * w[j][1] * w[k][2];
+                    float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
+                    float wg0 = W * g.x, wg1 = W * g.y, wg2 = W * g.z;
+                    nv3[0] += wg0;
+                    nv3[1] += wg1;
+                    nv3[2] += wg2;
+                    nC[0] += wg0 * d0; nC[1] += wg0 * d1; nC[2] += wg0 * d2;
+                    nC[3] += wg1 * d0; nC[4] += wg1 * d1; nC[5] += wg1 * d2;
+                    nC[6] += wg2 * d0; nC[7] += wg2 * d1; nC[8] += wg2 * d2;
+                }
+#pragma unroll
+        for (int i = 0; i < 9; ++i) nC[i] *= c4;
+        store9(a.next, a.stride, OC, p, nC);
+        float nx[3], outv[3];
+        if (kind == KIND_LIQUID) {
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                outv[cc] = nv3[cc];
+                nx[cc] = x[cc] + s.dt * nv3[cc];
+            }
+            bool fin = isfinite(nx[0]) && isfinite(nx[1]) && isfinite(nx[2]) && isfinite(nv3[0]) &&
+                       isfinite(nv3[1]) && isfinite(nv3[2]);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) fin = fin && isfinite(nC[i]);
+            any_nan = any_nan || !fin;
+        } else if (kind == KIND_ROD) {
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                dv[cc] += tv[cc] - nv3[cc];
+                outv[cc] = tv[cc];
+                nx[cc] = x[cc] + tv[cc] * s.dt;
+            }
+        } else {
+#pragma unroll
+            for (int cc = 0; cc < 3; ++cc) {
+                outv[cc] = 0.f;
+                nx[cc] = x[cc];
+            }
+        }
+        store3(a.next, a.stride, OV, p, outv);
+        store3(a.next, a.stride, OX, p, nx);
+    }
+    if (any_nan) atomicOr(a.status, DSTIR_STATUS_NAN);
+    if (s.rod_mode == DSTIR_ROD_PARTICLES && s.n_rod > 0) {
+        group_sum<3>(dv, sh, a.partial, a.counters + a.batch + br.scene, blockIdx.x - br.idx, br.count,
+                     a.force + br.scene * a.force_stride + (long long)a.fo * 3, s.force_scale);
+    }
+}
+
+// P2G adjoint with the brick's P/M adjoint nodes staged in shared memory.
+// Every brick CTA joins the deterministic per-scene parameter-gradient
+// reduction, empty bricks included.
+template <bool SVDJ>
+__global__ void __launch_bounds__(256) p2g_adj_brick_kernel(AdjArgs a, const BrickInfo* __restrict__ bricks,
+                                                            const int* __restrict__ cell_start,
+                                                            const int* __restrict__ perm, int n_bricks,
+                                                            long long nbins) {
+    __shared__ SceneDev s;
+    __shared__ BrickInfo br;
+    __shared__ BrickCtx ctx;
+    __shared__ float sh[32][4];
+    __shared__ float prm[4];
+    __shared__ int model;
+    __shared__ float4 gt[TILE_NODES];
+    if (blockIdx.x >= (unsigned)n_bricks) {
+        // overflow bin: no gather; only the stress / F_tmp adjoint of F[f+1]
+        int beg = cell_start[nbins], end = cell_start[nbins + 1];
+        const unsigned first = blockIdx.x - (unsigned)(gridDim.x - OVERFLOW_CTAS);
+        for (int q = beg + first * blockDim.x + threadIdx.x; q < end; q += OVERFLOW_CTAS * blockDim.x) {
+            long long p = perm[q];
+            int sc_i = 0;
+            while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
+            SceneDev s2 = a.sc[sc_i];
+            float pr[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) pr[i] = a.params[sc_i * 4 + i];
+            const int kind = particle_kind(s2, p);
+            float m, mv[3], A[9], Ab[9], vvb[3] = {0.f, 0.f, 0.f}, fxb[3] = {0.f, 0.f, 0.f}, pg[4] = {0.f, 0.f, 0.f, 0.f};
+            p2g_adj_affine<SVDJ>(a.cur, a.stride, s2, pr, a.models[sc_i], p, kind, m, mv, A);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ab[i] = 0.f;
+            p2g_adj_finish<SVDJ>(a, s2, pr, a.models[sc_i], p, kind, m, Ab, vvb, fxb, pg);
+        }
+        return;
+    }
+    brick_prologue(bricks, a.sc, cell_start, br, s, ctx);
+    if (threadIdx.x < 4) prm[threadIdx.x] = a.params[br.scene * 4 + threadIdx.x];
+    if (threadIdx.x == 0) model = a.models[br.scene];
+    const int oi = br.bi * 4, oj = br.bj * 4, ok = br.bk * 4;
+    if (ctx.cs[0] != ctx.cs[64])
+        for (int t = threadIdx.x; t < TILE_NODES; t += blockDim.x) {
+            const int gi = oi + t / (TILE * TILE), gj = oj + (t / TILE) % TILE, gk = ok + t % TILE;
+            gt[t] = (gi < s.n && gj < s.n && gk < s.n) ? __ldg(a.pmb + node_index(s, gi, gj, gk))
+                                                       : make_float4(0.f, 0.f, 0.f, 0.f);
+        }
+    __syncthreads();
+    float pg[4] = {0.f, 0.f, 0.f, 0.f};
+    const int nv = ctx.maxcnt * 64;
+    for (int v = threadIdx.x; v < nv; v += blockDim.x) {
+        const int c = v & 63, jv = v >> 6;
+        const int q = ctx.cs[c] + jv;
+        if (q >= ctx.cs[c + 1]) continue;
+        long long p = perm[q];
+        const int kind = particle_kind(s, p);
+        const bool liquid = kind == KIND_LIQUID;
+        float x[3];
+        load3(a.cur, a.stride, OX, p, x);
+        float m, mv[3], A[9];
+        p2g_adj_affine<SVDJ>(a.cur, a.stride, s, prm, model, p, kind, m, mv, A);
+        const int li = c >> 4, lj = (c >> 2) & 3, lk = c & 3;
+        float fx[3] = {x[0] * s.inv_dx - (float)(oi + li), x[1] * s.inv_dx - (float)(oj + lj),
+                       x[2] * s.inv_dx - (float)(ok + lk)};
+        float w[3][3], dw[3][3];
+        bspline_d(fx, w, dw);
+        float Ab[9], vvb[3] = {0.f, 0.f, 0.f}, fxb[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Ab[i] = 0.f;
+#pragma unroll
+        for (int i = 0; i < 3; ++i)
+#pragma unroll
+            for (int j = 0; j < 3; ++j)
+#pragma unroll
+                for (int k = 0; k < 3; ++k) {
+                    float dp[3] = {((float)i - fx[0]) * s.dx, ((float)j - fx[1]) * s.dx, ((float)k - fx[2]) * s.dx};
+                    p2g_adj_node(w[i][0] * w[j][1] * w[k][2], dw[i][0] * w[j][1] * w[k][2],
+                                 w[i][0] * dw[j][1] * w[k][2], w[i][0] * w[j][1] * dw[k][2], dp,
+                                 gt[tile_index(li + i, lj + j, lk + k)], m, mv, A, s.dx, liquid, Ab, vvb, fxb);
+                }
+        p2g_adj_finish<SVDJ>(a, s, prm, model, p, kind, m, Ab, vvb, fxb, pg);
+    }
+    group_sum<4>(pg, sh, a.partial, a.counters + 2 * a.batch + br.scene, blockIdx.x - br.idx, br.count,
+                 a.pgrad + ((long long)a.fo * a.batch + br.scene) * 4, 1.f);
+}
+
+void launch_g2p_brick(const FwdArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                      const int* perm, long long nbins, cudaStream_t st) {
+    if (n_bricks > 0) g2p_brick_kernel<<<n_bricks + OVERFLOW_CTAS, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+}
+
+void launch_p2g_adj_brick(const AdjArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                          const int* perm, long long nbins, bool svdj, cudaStream_t st) {
     if (n_bricks <= 0) return;
     if (svdj)
-        p2g_brick_kernel<true><<<n_bricks + 1, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+        p2g_adj_brick_kernel<true><<<n_bricks + OVERFLOW_CTAS, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
     else
-        p2g_brick_kernel<false><<<n_bricks + 1, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+        p2g_adj_brick_kernel<false><<<n_bricks + OVERFLOW_CTAS, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+}
+
+template <int MODE>
+static void p2g_brick_mode(const FwdArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                           const int* perm, long long nbins, bool svdj, cudaStream_t st) {
+    const int g = n_bricks + OVERFLOW_CTAS;
+    if (svdj)
+        p2g_brick_kernel<true, MODE><<<g, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+    else
+        p2g_brick_kernel<false, MODE><<<g, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+}
+
+void launch_p2g_brick(const FwdArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                      const int* perm, long long nbins, bool svdj, int mode, cudaStream_t st) {
+    if (n_bricks <= 0) return;
+    if (mode == SCATTER_RED)
+        p2g_brick_mode<SCATTER_RED>(a, bricks, n_bricks, cell_start, perm, nbins, svdj, st);
+    else if (mode == SCATTER_GLOBAL)
+        p2g_brick_mode<SCATTER_GLOBAL>(a, bricks, n_bricks, cell_start, perm, nbins, svdj, st);
+    else
+        p2g_brick_mode<SCATTER_ATOM>(a, bricks, n_bricks, cell_start, perm, nbins, svdj, st);
 }
 
 void launch_g2p_adj_brick(const AdjArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
-                          const int* perm, long long nbins, cudaStream_t st) {
-    if (n_bricks > 0) g2p_adj_brick_kernel<<<n_bricks + 1, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+                          const int* perm, long long nbins, int mode, cudaStream_t st) {
+    if (n_bricks <= 0) return;
+    const int g = n_bricks + OVERFLOW_CTAS;
+    if (mode == SCATTER_RED)
+        g2p_adj_brick_kernel<SCATTER_RED><<<g, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+    else if (mode == SCATTER_GLOBAL)
+        g2p_adj_brick_kernel<SCATTER_GLOBAL><<<g, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
+    else
+        g2p_adj_brick_kernel<SCATTER_ATOM><<<g, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
 }
 
 void launch_p2g_cell(const FwdArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
                      long long G, bool svdj, cudaStream_t st) {
     if (n_gblocks <= 0) return;
     if (svdj)
-        p2g_cell_kernel<true><<<n_gblocks + 1, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
+        p2g_cell_kernel<true><<<n_gblocks + OVERFLOW_CTAS, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
     else
-        p2g_cell_kernel<false><<<n_gblocks + 1, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
+        p2g_cell_kernel<false><<<n_gblocks + OVERFLOW_CTAS, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
 }
 
 void launch_g2p_adj_cell(const AdjArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
                          long long G, cudaStream_t st) {
-    if (n_gblocks > 0) g2p_adj_cell_kernel<<<n_gblocks + 1, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
+    if (n_gblocks > 0) g2p_adj_cell_kernel<<<n_gblocks + OVERFLOW_CTAS, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
 }
 
 }  // namespace dstir

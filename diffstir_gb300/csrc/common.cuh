@@ -105,7 +105,7 @@ __device__ __forceinline__ long long brick_key(const SceneDev& s, int i, int j, 
 struct BrickInfo {
     int scene, bi, bj, bk;
     long long key0;
-    long long pad;
+    int idx, count;  // rank of the brick among the scene's bricks, and their number
 };
 
 __device__ __forceinline__ void matmul3(const float* A, const float* B, float* o) {

@@ -94,10 +94,16 @@ void launch_p2g_cell(const FwdArgs& a, const int* cell_start, const int* perm, i
 void launch_g2p_adj_cell(const AdjArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
                          long long G, cudaStream_t st);
 
+// scatter mode of the brick kernels: 0 shared tile + atomicAdd, 1 shared tile +
+// red.shared, 2 direct global vector atomics in the brick's lane order
 void launch_p2g_brick(const FwdArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
-                      const int* perm, long long nbins, bool svdj, cudaStream_t st);
+                      const int* perm, long long nbins, bool svdj, int mode, cudaStream_t st);
 void launch_g2p_adj_brick(const AdjArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
-                          const int* perm, long long nbins, cudaStream_t st);
+                          const int* perm, long long nbins, int mode, cudaStream_t st);
+void launch_g2p_brick(const FwdArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                      const int* perm, long long nbins, cudaStream_t st);
+void launch_p2g_adj_brick(const AdjArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,
+                          const int* perm, long long nbins, bool svdj, cudaStream_t st);
 
 void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
                        long long stride, long long n, cudaStream_t s);

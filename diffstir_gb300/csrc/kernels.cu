@@ -18,6 +18,7 @@
 #include "internal.h"
 #include "svd.cuh"
 #include "device_util.cuh"
+#include "adjoint.cuh"
 
 namespace dstir {
 
@@ -415,10 +416,7 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(AdjArgs a) {
     a.pmb[node] = make_float4(inv_m * ub[0], inv_m * ub[1], inv_m * ub[2], mb - inv_m * inv_m * Pu);
 }
 
-// P2G adjoint in three phases so that few values stay live across the 27-node
-// gather: (1) recompute the particle's affine momentum A and m*v' (as in the
-// forward), (2) gather the P/M adjoint over the stencil, (3) reload C and F and
-// run the stress / bulk / viscosity / F_tmp adjoints.
+// P2G adjoint, one thread per particle (pieces in adjoint.cuh).
 template <bool SVDJ>
 __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
     __shared__ SceneDev s;
@@ -434,36 +432,13 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
     }
     __syncthreads();
     long long p = bi.start + threadIdx.x;
-    bool active = p < bi.end;
     float pg[4] = {0.f, 0.f, 0.f, 0.f};
-    if (active) {
+    if (p < bi.end) {
         const bool liquid = bi.kind == KIND_LIQUID;
         float x[3];
         load3(a.cur, a.stride, OX, p, x);
         float m, mv[3], A[9];
-        {  // phase 1
-            float v[3], C[9];
-            load3(a.cur, a.stride, OV, p, v);
-            load9(a.cur, a.stride, OC, p, C);
-            if (liquid) {
-                float F[9];
-                load9(a.cur, a.stride, OF, p, F);
-                LiquidP2G q;
-                liquid_p2g<SVDJ>(s, model, prm, v, C, F, q);
-                m = s.m_liq;
-#pragma unroll
-                for (int i = 0; i < 9; ++i) A[i] = q.A[i];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) mv[c] = m * q.vv[c];
-            } else {
-                m = (bi.kind == KIND_ROD) ? s.m_rod : s.m_cont;
-#pragma unroll
-                for (int i = 0; i < 9; ++i) A[i] = m * C[i];
-#pragma unroll
-                for (int c = 0; c < 3; ++c) mv[c] = m * v[c];
-            }
-        }
-        // phase 2: gather of the P/M adjoint
+        p2g_adj_affine<SVDJ>(a.cur, a.stride, s, prm, model, p, bi.kind, m, mv, A);
         float Ab[9], vvb[3] = {0.f, 0.f, 0.f}, fxb[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int i = 0; i < 9; ++i) Ab[i] = 0.f;
@@ -479,129 +454,15 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
                     long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        float4 gb = __ldg(a.pmb + row + k);
-                        float W = w[i][0] * w[j][1] * w[k][2];
                         float dp[3] = {((float)i - fx[0]) * s.dx, ((float)j - fx[1]) * s.dx,
                                        ((float)k - fx[2]) * s.dx};
-                        float gbv[3] = {gb.x, gb.y, gb.z};
-                        float Wb = gb.w * m;
-#pragma unroll
-                        for (int aa = 0; aa < 3; ++aa) {
-                            float ad = A[aa * 3 + 0] * dp[0] + A[aa * 3 + 1] * dp[1] + A[aa * 3 + 2] * dp[2];
-                            Wb += gbv[aa] * (mv[aa] + ad);
-                            vvb[aa] += W * gbv[aa];
-#pragma unroll
-                            for (int bb = 0; bb < 3; ++bb) Ab[aa * 3 + bb] += W * gbv[aa] * dp[bb];
-                        }
-                        if (liquid) {
-#pragma unroll
-                            for (int bb = 0; bb < 3; ++bb)
-                                fxb[bb] -= W * s.dx *
-                                           (A[0 * 3 + bb] * gbv[0] + A[1 * 3 + bb] * gbv[1] + A[2 * 3 + bb] * gbv[2]);
-                            fxb[0] += Wb * dw[i][0] * w[j][1] * w[k][2];
-                            fxb[1] += Wb * w[i][0] * dw[j][1] * w[k][2];
-                            fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
-                        }
+                        p2g_adj_node(w[i][0] * w[j][1] * w[k][2], dw[i][0] * w[j][1] * w[k][2],
+                                     w[i][0] * dw[j][1] * w[k][2], w[i][0] * w[j][1] * dw[k][2], dp,
+                                     __ldg(a.pmb + row + k), m, mv, A, s.dx, liquid, Ab, vvb, fxb);
                     }
                 }
         }
-#pragma unroll
-        for (int c = 0; c < 3; ++c) vvb[c] *= m;
-        // phase 3
-        if (!liquid) {
-            float Cb[9], z[9];
-#pragma unroll
-            for (int i = 0; i < 9; ++i) {
-                Cb[i] = m * Ab[i];
-                z[i] = 0.f;
-            }
-            store3(a.adj_cur, a.stride, OX, p, z);
-            store3(a.adj_cur, a.stride, OV, p, z);
-            store9(a.adj_cur, a.stride, OC, p, Cb);
-            store9(a.adj_cur, a.stride, OF, p, z);
-        } else {
-            float xb[3];
-            load3(a.adj_cur, a.stride, OX, p, xb);  // G2P part, written by the G2P adjoint
-#pragma unroll
-            for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
-            store3(a.adj_cur, a.stride, OX, p, xb);
-            store3(a.adj_cur, a.stride, OV, p, vvb);
-            float C[9], F[9], IC[9], Ft[9];
-            load9(a.cur, a.stride, OC, p, C);
-            load9(a.cur, a.stride, OF, p, F);
-#pragma unroll
-            for (int i = 0; i < 9; ++i) IC[i] = s.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
-            matmul3(IC, F, Ft);
-            float U[9], sg[3], Vm[9], J;
-            if (SVDJ && s.j_mode == DSTIR_J_SVD) {
-                svd3(Ft, U, sg, Vm);
-                J = sg[0] * sg[1] * sg[2];
-            } else {
-                J = det3(Ft);
-            }
-            float nrm2 = 0.f;
-#pragma unroll
-            for (int i = 0; i < 9; ++i) nrm2 += C[i] * C[i];
-            float nrm = sqrtf(nrm2);
-            Visc vs = viscosity<true>(model, prm, nrm + 1e-6f);
-            float Cb[9], sigb[9];
-#pragma unroll
-            for (int i = 0; i < 9; ++i) {
-                Cb[i] = m * Ab[i];
-                sigb[i] = s.alpha * Ab[i];
-            }
-            float etab = 0.f;
-#pragma unroll
-            for (int aa = 0; aa < 3; ++aa)
-#pragma unroll
-                for (int bb = 0; bb < 3; ++bb) {
-                    float Dab = 0.5f * (C[aa * 3 + bb] + C[bb * 3 + aa]);
-                    etab += sigb[aa * 3 + bb] * Dab;
-                    Cb[aa * 3 + bb] += vs.eta * 0.5f * (sigb[aa * 3 + bb] + sigb[bb * 3 + aa]);
-                }
-            float trb = sigb[0] + sigb[4] + sigb[8];
-            float Jb = trb * (s.bulk / 2.f) * (2.f * J - 1.f);
-            float Ftb[9];
-            load9(a.adj_next, a.stride, OF, p, Ftb);  // F[f+1] = F_tmp
-            if (SVDJ && s.j_mode == DSTIR_J_SVD) {
-                float gS[3] = {Jb * sg[1] * sg[2], Jb * sg[0] * sg[2], Jb * sg[0] * sg[1]};
-                float z[9], gA[9];
-#pragma unroll
-                for (int i = 0; i < 9; ++i) z[i] = 0.f;
-                svd3_backward(z, gS, z, U, sg, Vm, gA);
-#pragma unroll
-                for (int i = 0; i < 9; ++i) Ftb[i] += gA[i];
-            } else {
-                float cf[9];
-                cof3(Ft, cf);
-#pragma unroll
-                for (int i = 0; i < 9; ++i) Ftb[i] += Jb * cf[i];
-            }
-            float gammab = etab * vs.deta_dgamma;
-#pragma unroll
-            for (int i = 0; i < 4; ++i) pg[i] = etab * vs.dp[i];
-            if (nrm > 0.f) {
-                float inv = gammab / nrm;
-#pragma unroll
-                for (int i = 0; i < 9; ++i) Cb[i] += inv * C[i];
-            }
-            float Fb[9];
-#pragma unroll
-            for (int aa = 0; aa < 3; ++aa)
-#pragma unroll
-                for (int bb = 0; bb < 3; ++bb) {
-                    float sF = 0.f, sC = 0.f;
-#pragma unroll
-                    for (int c = 0; c < 3; ++c) {
-                        sF += IC[c * 3 + aa] * Ftb[c * 3 + bb];
-                        sC += Ftb[aa * 3 + c] * F[bb * 3 + c];
-                    }
-                    Fb[aa * 3 + bb] = sF;
-                    Cb[aa * 3 + bb] += s.dt * sC;
-                }
-            store9(a.adj_cur, a.stride, OC, p, Cb);
-            store9(a.adj_cur, a.stride, OF, p, Fb);
-        }
+        p2g_adj_finish<SVDJ>(a, s, prm, model, p, bi.kind, m, Ab, vvb, fxb, pg);
     }
     if (bi.kind == KIND_LIQUID) {
         group_sum<4>(pg, sh, a.partial, a.counters + 2 * a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,

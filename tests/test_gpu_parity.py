@@ -64,8 +64,10 @@ def fixture_scene(name, model):
                  d['operator_trajectory'], d['m%d_params' % model]), d
 
 
-VARIANTS = [{'p2g': 1}, {'p2g': 2}, {'p2g': 3}, {'p2g': 3, 'graph': 1}]
-VARIANT_IDS = ['vec-atomics', 'cell-binned', 'brick-tiled', 'brick-graph']
+VARIANTS = [{'p2g': 1}, {'p2g': 2}, {'p2g': 3}, {'p2g': 3, 'brick_scatter': 0}, {'p2g': 3, 'brick_scatter': 2},
+            {'p2g': 3, 'brick_gather': 0}, {'p2g': 3, 'graph': 1}]
+VARIANT_IDS = ['vec-atomics', 'cell-binned', 'brick-red', 'brick-atom', 'brick-global', 'brick-nogather',
+               'brick-graph']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
