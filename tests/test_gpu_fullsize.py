@@ -89,4 +89,4 @@ def test_full_size_gravity_only_substep():
     np.testing.assert_allclose(v[:, 0], 0.0, atol=1e-9)
     np.testing.assert_allclose(v[:, 2], 0.0, atol=1e-9)
     assert np.all(v[:, 1] <= 0.0) and np.all(v[:, 1] >= g * (1 + 1e-5))
-    assert abs(np.median(v[:, 1]) - g) < 1e-5 * abs(g)
+    assert abs(np.median(v[:, 1]) - g) < 1e-4 * abs(g)   # 1e-10 mass floor / ~4e-6 node mass
