@@ -42,11 +42,18 @@ UNIT = 'particle-substeps/s'
 # g2p_adj: read x (12), adj x,v,C (60), write adj x (12); read v 12, write grid adjoint 12 per node
 # grid_adj: read P,M 16, grid adjoint 12, write P/M adjoint 16, clear 12
 # p2g_adj: read state 96, adj F 36, adj x 12, write adj state 96; read P/M adjoint 16 per node
+# g2p_p2g (G2P of substep f fused with P2G of f+1): read x (12), F (36), write
+#   x,v,C (60), F (36); read v grid 12/node, P2G result 16/node
 KERNEL_BYTES = {
     'p2g': (132, 16), 'grid': (0, 44), 'g2p': (72, 12),
     'g2p_adj': (84, 24), 'grid_adj': (0, 56), 'p2g_adj': (240, 16),
+    'g2p_p2g': (144, 28),
+    # p2g_adj_g2p_adj (P2G adjoint of f fused with the G2P adjoint of f-1): read
+    #   state f (96), adj F (36), adj x part (12), x of f-1 (12); write adj F (36),
+    #   adj x part of f-1 (12); read P/M adjoint 16 + velocity 12, write grid adjoint 12 per node
+    'p2g_adj_g2p_adj': (204, 40),
 }
-KERNELS = ['p2g', 'grid', 'g2p', 'g2p_adj', 'grid_adj', 'p2g_adj', 'bin', 'other']
+KERNELS = ['p2g', 'grid', 'g2p', 'g2p_adj', 'grid_adj', 'p2g_adj', 'bin', 'g2p_p2g', 'p2g_adj_g2p_adj', 'other']
 
 
 def parse():
@@ -66,6 +73,8 @@ def parse():
     ap.add_argument('--autotune', type=int, default=1, help='1: launch options from the autotuner (cached)')
     ap.add_argument('--brick-scatter', type=int, default=None, help='brick P2G scatter: 0 atom, 1 red.shared, 2 global')
     ap.add_argument('--brick-gather', type=int, default=None)
+    ap.add_argument('--fuse', type=int, default=None, help='1: G2P(f) fused with P2G(f+1)')
+    ap.add_argument('--fuse-adj', type=int, default=None, help='1: P2G adjoint of f fused with G2P adjoint of f-1')
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')
@@ -236,7 +245,7 @@ def run_ours(args):
     scenes, T, ckpt = build_workload(args, rank)
     sc = scenes[0]
     opts = {}
-    keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather')
+    keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather', 'fuse', 'fuse_adj')
     explicit = any(getattr(args, k) is not None for k in keys)
     if args.autotune and not explicit:
         from diffstir_gb300 import autotune
@@ -252,7 +261,9 @@ def run_ours(args):
     ys = S_yield(args.config)
 
     # target force profiles from seeded ground-truth parameters
-    true_p = torch.tensor(np.stack([S.draw_params(rng, ys) for _ in range(B)]), dtype=torch.float32, device=dev)
+    nr = S.config_n_range(args.config)
+    true_p = torch.tensor(np.stack([S.draw_params(rng, ys, nr) for _ in range(B)]), dtype=torch.float32,
+                          device=dev)
     sim.set_params(true_p)
     sim.reset()
     target = sim.forward(T).clone()
@@ -403,7 +414,8 @@ def run_ours(args):
         'cpu_baseline': cpu,
         'e2e': e2e,
         'gpu_launches': int(launches),
-        'options': {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather')},
+        'options': {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather',
+                                                   'fuse', 'fuse_adj')},
         'clocks': clk,
         'status_flags': int(st),
     }

@@ -154,8 +154,7 @@ class _InitialPositions:
         else:
             sc.container_x = arr.copy()
         if _state.sim is not None:
-            import torch
-            _state.sim._x0 = torch.from_numpy(sc.x0()).float().to(_state.sim.device)
+            _state.sim.set_x0(sc.x0())
 
     def to_numpy(self):
         sc = _sc
@@ -234,7 +233,7 @@ def _ensure_sim():
         sim = Simulator(_sc, max_steps=max_steps - 1)
         _state.sim = sim
         _state.hist_x = torch.zeros((max_steps, sim.N, 3), device=sim.device)
-        _state.hist_x[0] = sim._x0
+        _state.hist_x[0] = sim.get_state()['x']
     return _state.sim
 
 
@@ -257,7 +256,7 @@ def initialize_ti_field():
     """simulation_functions.py:301-319: step-0 state, zero total_operator_dv."""
     sim = _ensure_sim()
     sim.reset()
-    _state.hist_x[0] = sim._x0
+    _state.hist_x[0] = sim.get_state()['x']
     _state.total_dv[...] = 0
     _state.forces = {}
     _state.pending = []

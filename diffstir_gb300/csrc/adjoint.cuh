@@ -67,31 +67,28 @@ __device__ __forceinline__ void p2g_adj_node(float W, float dWx, float dWy, floa
     }
 }
 
+// The adjoint of the state at substep f (xb, vb, Cb, Fb) from the stencil
+// gather results; parameter partials are added to pg.
 template <bool SVDJ>
-__device__ __forceinline__ void p2g_adj_finish(const AdjArgs& a, const SceneDev& s, const float* prm, int model,
-                                               long long p, int kind, float m, const float Ab[9], float vvb[3],
-                                               const float fxb[3], float pg[4]) {
+__device__ __forceinline__ void p2g_adj_core(const AdjArgs& a, const SceneDev& s, const float* prm, int model,
+                                             long long p, int kind, float m, const float Ab[9], const float vvb[3],
+                                             const float fxb[3], float pg[4], float xb[3], float vb[3], float Cb[9],
+                                             float Fb[9]) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) vvb[c] *= m;
+    for (int c = 0; c < 3; ++c) vb[c] = vvb[c] * m;
     if (kind != KIND_LIQUID) {
-        float Cb[9], z[9];
 #pragma unroll
         for (int i = 0; i < 9; ++i) {
             Cb[i] = m * Ab[i];
-            z[i] = 0.f;
+            Fb[i] = 0.f;
         }
-        store3(a.adj_cur, a.stride, OX, p, z);
-        store3(a.adj_cur, a.stride, OV, p, z);
-        store9(a.adj_cur, a.stride, OC, p, Cb);
-        store9(a.adj_cur, a.stride, OF, p, z);
+#pragma unroll
+        for (int c = 0; c < 3; ++c) xb[c] = vb[c] = 0.f;
         return;
     }
-    float xb[3];
     load3(a.adj_cur, a.stride, OX, p, xb);  // G2P part, written by the G2P adjoint
 #pragma unroll
     for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
-    store3(a.adj_cur, a.stride, OX, p, xb);
-    store3(a.adj_cur, a.stride, OV, p, vvb);
     float C[9], F[9], IC[9], Ft[9];
     load9(a.cur, a.stride, OC, p, C);
     load9(a.cur, a.stride, OF, p, F);
@@ -110,7 +107,7 @@ __device__ __forceinline__ void p2g_adj_finish(const AdjArgs& a, const SceneDev&
     for (int i = 0; i < 9; ++i) nrm2 += C[i] * C[i];
     float nrm = sqrtf(nrm2);
     Visc vs = viscosity<true>(model, prm, nrm + 1e-6f);
-    float Cb[9], sigb[9];
+    float sigb[9];
 #pragma unroll
     for (int i = 0; i < 9; ++i) {
         Cb[i] = m * Ab[i];
@@ -151,7 +148,6 @@ __device__ __forceinline__ void p2g_adj_finish(const AdjArgs& a, const SceneDev&
 #pragma unroll
         for (int i = 0; i < 9; ++i) Cb[i] += inv * C[i];
     }
-    float Fb[9];
 #pragma unroll
     for (int aa = 0; aa < 3; ++aa)
 #pragma unroll
@@ -165,6 +161,17 @@ __device__ __forceinline__ void p2g_adj_finish(const AdjArgs& a, const SceneDev&
             Fb[aa * 3 + bb] = sF;
             Cb[aa * 3 + bb] += s.dt * sC;
         }
+}
+
+// p2g_adj_core followed by storing the whole state adjoint into a.adj_cur.
+template <bool SVDJ>
+__device__ __forceinline__ void p2g_adj_finish(const AdjArgs& a, const SceneDev& s, const float* prm, int model,
+                                               long long p, int kind, float m, const float Ab[9], float vvb[3],
+                                               const float fxb[3], float pg[4]) {
+    float xb[3], vb[3], Cb[9], Fb[9];
+    p2g_adj_core<SVDJ>(a, s, prm, model, p, kind, m, Ab, vvb, fxb, pg, xb, vb, Cb, Fb);
+    store3(a.adj_cur, a.stride, OX, p, xb);
+    store3(a.adj_cur, a.stride, OV, p, vb);
     store9(a.adj_cur, a.stride, OC, p, Cb);
     store9(a.adj_cur, a.stride, OF, p, Fb);
 }

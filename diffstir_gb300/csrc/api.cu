@@ -24,8 +24,11 @@ using namespace dstir;
 
 namespace {
 // kernel kinds timed by the optional in-library profiler
-enum { K_P2G = 0, K_GRID, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_BIN, K_OTHER, K_NUM };
-const char* const kKernelNames[K_NUM] = {"p2g", "grid", "g2p", "g2p_adj", "grid_adj", "p2g_adj", "bin", "other"};
+enum { K_P2G = 0, K_GRID, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_BIN, K_G2P_P2G, K_P2G_ADJ_G2P_ADJ, K_OTHER,
+       K_NUM };
+const char* const kKernelNames[K_NUM] = {"p2g",     "grid",    "g2p",                "g2p_adj", "grid_adj",
+                                         "p2g_adj", "bin",     "g2p_p2g",            "p2g_adj_g2p_adj",
+                                         "other"};
 
 // CUDA-event timing of every launch on the launching stream.  Event pairs live
 // in a ring; a pair is read back (synchronising on its stop event) when the
@@ -107,6 +110,8 @@ struct DstirHandle {
     int block = 256, gblock = 256, p2g_variant = P2G_VEC, use_graph = 0;
     int brick_gather = 1;   // with P2G_BRICK: G2P and the P2G adjoint also gather from brick tiles
     int brick_scatter = 1;  // with P2G_BRICK: 0 shared atomics, 1 shared red, 2 direct global atomics
+    int fuse = 1;           // per-particle variants: G2P(f) and P2G(f+1) in one kernel
+    int fuse_adj = 1;       // per-particle variants: P2G adjoint of f and G2P adjoint of f-1 in one kernel
     std::vector<BlockInfo> blk_h;
     std::vector<GridBlock> gblk_h;
     SceneDev* sc = nullptr;
@@ -114,7 +119,7 @@ struct DstirHandle {
     GridBlock* gblk = nullptr;
     int n_blocks = 0, n_gblocks = 0;
 
-    float* work = nullptr;   // 2 state slots
+    float* work = nullptr;   // 3 state slots (states f, f+1, f+2 of the fused substep)
     float* ckpt = nullptr;
     long long ckpt_slots = 0;
     float* seg = nullptr;
@@ -297,6 +302,8 @@ FwdArgs fwd_args(DstirHandle* h, const float* cur, float* next, float4* pm, floa
     a.status = h->status;
     a.clear_pm = clear_pm;
     a.batch = h->B;
+    a.next2 = nullptr;
+    a.pm_next = nullptr;
     return a;
 }
 
@@ -487,7 +494,7 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
     std::vector<int> models(batch);
     for (int s = 0; s < batch; ++s) models[s] = scenes[s].model;
     if ((rc = dalloc(h, &h->sc, batch, "scene table")) ||
-        (rc = dalloc(h, &h->work, 2 * slot_floats(h), "state")) ||
+        (rc = dalloc(h, &h->work, 3 * slot_floats(h), "state")) ||
         (rc = dalloc(h, &h->adj, 2 * slot_floats(h), "adjoint state")) ||
         (rc = dalloc(h, &h->ga, (size_t)h->G, "grid adjoint")) ||
         (rc = dalloc(h, &h->pmb, (size_t)h->G, "P2G adjoint")) ||
@@ -515,7 +522,7 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
     if (e == cudaSuccess) e = cudaMemset(h->ga, 0, (size_t)h->G * sizeof(float4));
     if (e == cudaSuccess) e = cudaMemset(h->params, 0, (size_t)batch * 4 * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(h->traj, 0, (size_t)batch * (max_steps + 1) * 3 * sizeof(float));
-    if (e == cudaSuccess) e = cudaMemset(h->work, 0, 2 * slot_floats(h) * sizeof(float));
+    if (e == cudaSuccess) e = cudaMemset(h->work, 0, 3 * slot_floats(h) * sizeof(float));
     if (e != cudaSuccess) {
         dstir_destroy(h);
         return DSTIR_ECUDA;
@@ -597,20 +604,67 @@ namespace {
 
 // Enqueue a forward rollout; forces go to h->fbuf [B][max_steps][3] at fo = k.
 // Returns the work slot that holds the final state.
+bool fused(const DstirHandle* h) { return h->fuse && !binned(h); }
+bool fused_adj(const DstirHandle* h) { return h->fuse_adj && !binned(h); }
+
+// Forward chain of `nsteps` substeps over the state slots slot(0..nsteps).
+// With fusion: P2G(0), then per substep k the grid update and G2P(k) fused
+// with P2G(k+1); the last substep ends with a plain G2P unless `skip_last_g2p`.
+template <class SlotFn, class GridFn>
+void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids, float* force,
+                   long long fstride, int fo0, int clear_pm, bool skip_last_g2p, cudaStream_t st) {
+    if (!fused(h)) {
+        for (int k = 0; k < nsteps; ++k) {
+            float4 *pm, *vo;
+            grids(k, pm, vo);
+            FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + k, force, fstride, fo0 + k, clear_pm);
+            run_substep(h, a, st, k);
+        }
+        return;
+    }
+    {
+        float4 *pm, *vo;
+        grids(0, pm, vo);
+        FwdArgs a = fwd_args(h, slot(0), slot(1), pm, vo, t0, force, fstride, fo0, clear_pm);
+        timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st); });
+    }
+    for (int k = 0; k < nsteps; ++k) {
+        float4 *pm, *vo;
+        grids(k, pm, vo);
+        FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + k, force, fstride, fo0 + k, clear_pm);
+        timed(h, K_GRID, st, [&] { launch_grid(a, h->n_gblocks, h->gblock, st); });
+        if (k + 1 < nsteps) {
+            float4 *pmn, *von;
+            grids(k + 1, pmn, von);
+            a.next2 = slot(k + 2);
+            a.pm_next = pmn;
+            timed(h, K_G2P_P2G, st,
+                  [&] { launch_g2p_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st); });
+        } else if (!skip_last_g2p) {
+            timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st); });
+        }
+    }
+}
+
+// Enqueue a forward rollout; forces go to h->fbuf [B][max_steps][3] at fo = k.
+// State k lives in checkpoint slot k/K when recording and k is a multiple of
+// K, else in work slot (cur + k) % 3; returns the work slot of the final state.
 int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, cudaStream_t st) {
     size_t sf = slot_floats(h);
-    float* W[2] = {h->work, h->work + sf};
-    float* curp = W[h->cur];
-    if (record) cudaMemcpyAsync(h->ckpt, curp, sf * sizeof(float), cudaMemcpyDeviceToDevice, st);
+    float* W[3] = {h->work, h->work + sf, h->work + 2 * sf};
+    const int cur = h->cur;
+    auto slot = [&](int k) -> float* {
+        if (record && k % K == 0 && k < nsteps) return h->ckpt + (size_t)(k / K) * sf;
+        return W[(cur + k) % 3];
+    };
+    if (record) cudaMemcpyAsync(h->ckpt, W[cur], sf * sizeof(float), cudaMemcpyDeviceToDevice, st);
     cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st);
-    for (int k = 0; k < nsteps; ++k) {
-        bool boundary = record && ((k + 1) % K == 0) && (k + 1 < nsteps);
-        float* dst = boundary ? h->ckpt + (size_t)((k + 1) / K) * sf : (curp == W[0] ? W[1] : W[0]);
-        FwdArgs a = fwd_args(h, curp, dst, h->pm, h->vo, t0 + k, h->fbuf, (long long)h->max_steps * 3, k, 1);
-        run_substep(h, a, st);
-        curp = dst;
-    }
-    return (curp == W[0]) ? 0 : 1;
+    auto grids = [&](int, float4*& pm, float4*& vo) {
+        pm = h->pm;
+        vo = h->vo;
+    };
+    chain_forward(h, t0, nsteps, slot, grids, h->fbuf, (long long)h->max_steps * 3, 0, 1, false, st);
+    return (cur + nsteps) % 3;
 }
 
 // Run `body(stream)` either directly on `st` or as a cached CUDA graph
@@ -677,22 +731,13 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
         h->ckpt_slots = nseg;
     }
     if (binned(h) && (rc = ensure_bin_slots(h, 1))) return rc;
-    long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch, h->p2g_variant, h->block * 4096 + h->gblock};
+    long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch, h->p2g_variant * 16 + h->fuse,
+                         h->block * 4096 + h->gblock};
     int final_slot = 0;
     rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want,
                          [&](cudaStream_t s2) { final_slot = enqueue_forward(h, t0, nsteps, K, record != 0, s2); });
     if (rc) return rc;
-    if (h->use_graph) {
-        // the slot sequence is fixed by (cur, nsteps, K, record): replay it on the host
-        size_t sf = slot_floats(h);
-        float* W[2] = {h->work, h->work + sf};
-        float* curp = W[h->cur];
-        for (int k = 0; k < nsteps; ++k) {
-            bool boundary = record && ((k + 1) % K == 0) && (k + 1 < nsteps);
-            curp = boundary ? h->ckpt + (size_t)((k + 1) / K) * sf : (curp == W[0] ? W[1] : W[0]);
-        }
-        final_slot = (curp == W[0]) ? 0 : 1;
-    }
+    final_slot = (h->cur + nsteps) % 3;  // also when the chain ran as a replayed graph
     h->cur = final_slot;
     if (force_out)
         CUDA_TRY(h, cudaMemcpy2DAsync(force_out, (size_t)nsteps * 3 * sizeof(float), h->fbuf,
@@ -715,14 +760,14 @@ int dstir_substep(DstirHandle* h, int32_t f, float* force_out, void* stream) {
     int rc;
     if (binned(h) && (rc = ensure_bin_slots(h, 1))) return rc;
     size_t sf = slot_floats(h);
-    float* W[2] = {h->work, h->work + sf};
+    float* W[3] = {h->work, h->work + sf, h->work + 2 * sf};
     float* force = force_out ? force_out : h->force_scratch;
     long long fstride = force_out ? 3 : (long long)h->max_steps * 3;
     int fo = force_out ? 0 : f;
-    FwdArgs a = fwd_args(h, W[h->cur], W[1 - h->cur], h->pm, h->vo, f, force, fstride, fo, 1);
+    FwdArgs a = fwd_args(h, W[h->cur], W[(h->cur + 1) % 3], h->pm, h->vo, f, force, fstride, fo, 1);
     run_substep(h, a, st);
     CUDA_TRY(h, cudaGetLastError());
-    h->cur = 1 - h->cur;
+    h->cur = (h->cur + 1) % 3;
     return DSTIR_OK;
 }
 
@@ -738,8 +783,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
     const long long nseg = (n + K - 1) / K;
     size_t sf = slot_floats(h);
     float* A[2] = {h->adj, h->adj + sf};
-    int nx = 0;
-    cudaMemsetAsync(A[nx], 0, sf * sizeof(float), st);
+    cudaMemsetAsync(A[0], 0, sf * sizeof(float), st);  // adjoint of the final state: zero
     cudaMemsetAsync(h->ga, 0, (size_t)h->G * sizeof(float4), st);
     cudaMemsetAsync(h->pgrad, 0, (size_t)n * h->B * 4 * sizeof(float), st);
     for (long long sgi = nseg - 1; sgi >= 0; --sgi) {
@@ -748,12 +792,16 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
         float* slot0 = h->ckpt + (size_t)sgi * sf;
         auto slot = [&](int j) -> float* { return j == 0 ? slot0 : h->seg + (size_t)(j - 1) * sf; };
         cudaMemsetAsync(h->pm, 0, (size_t)L * h->G * sizeof(float4), st);
-        for (int k = 0; k < L; ++k) {
-            FwdArgs a = fwd_args(h, slot(k), slot(k + 1), h->pm + (size_t)k * h->G, h->vo + (size_t)k * h->G,
-                                 t0 + s0 + k, h->force_scratch, (long long)h->max_steps * 3, t0 + s0 + k, 0);
-            run_substep(h, a, st, k);
-        }
-        for (int k = L - 1; k >= 0; --k) {
+        auto grids = [&](int k, float4*& pm, float4*& vo) {
+            pm = h->pm + (size_t)k * h->G;
+            vo = h->vo + (size_t)k * h->G;
+        };
+        // recompute the segment, keeping every state and grid; the state after
+        // its last substep is not needed by the adjoint
+        chain_forward(h, t0 + s0, L, slot, grids, h->force_scratch, (long long)h->max_steps * 3, t0 + s0, 0, true,
+                      st);
+        // adjoint of the state at global step g (relative to t0) lives in A[(n - g) & 1]
+        auto adj_args = [&](int k) {
             AdjArgs a;
             a.sc = h->sc;
             a.blk = h->blk;
@@ -764,8 +812,8 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.vo = h->vo + (size_t)k * h->G;
             a.ga = h->ga;
             a.pmb = h->pmb;
-            a.adj_next = A[nx];
-            a.adj_cur = A[1 - nx];
+            a.adj_next = A[(n - (s0 + k + 1)) & 1];
+            a.adj_cur = A[(n - (s0 + k)) & 1];
             a.traj = h->traj;
             a.traj_len = h->max_steps + 1;
             a.f = t0 + s0 + k;
@@ -778,13 +826,41 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.partial = h->partial;
             a.counters = h->counters;
             a.batch = h->B;
-            run_adj_substep(h, a, st, k);
-            nx = 1 - nx;
+            a.cur2 = nullptr;
+            a.vo2 = nullptr;
+            a.adj_prev = nullptr;
+            return a;
+        };
+        if (!fused_adj(h)) {
+            for (int k = L - 1; k >= 0; --k) run_adj_substep(h, adj_args(k), st, k);
+        } else {
+            // G2P adjoint of the segment's last substep, then per substep k the
+            // grid adjoint and the P2G adjoint of k fused with the G2P adjoint of
+            // k-1; the first substep of the segment ends with a plain P2G adjoint
+            // that stores the whole state adjoint for the previous segment
+            const int var = h->p2g_variant == P2G_PLAIN ? P2G_PLAIN : P2G_VEC;
+            {
+                AdjArgs a = adj_args(L - 1);
+                timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st); });
+            }
+            for (int k = L - 1; k >= 0; --k) {
+                AdjArgs a = adj_args(k);
+                timed(h, K_GRID_ADJ, st, [&] { launch_grid_adj(a, h->n_gblocks, h->gblock, st); });
+                if (k >= 1) {
+                    a.cur2 = slot(k - 1);
+                    a.vo2 = h->vo + (size_t)(k - 1) * h->G;
+                    a.adj_prev = A[(n - (s0 + k - 1)) & 1];
+                    timed(h, K_P2G_ADJ_G2P_ADJ, st,
+                          [&] { launch_p2g_adj_g2p_adj(a, h->n_blocks, h->block, var, h->any_svd, st); });
+                } else {
+                    timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st); });
+                }
+            }
         }
     }
     cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st);
     timed(h, K_OTHER, st, [&] { launch_reduce_pgrad(h->pgrad, n, h->B, h->dpbuf, st); });
-    return nx;
+    return n & 1;
 }
 
 }  // namespace
@@ -810,7 +886,8 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
     CUDA_TRY(h, cudaMemcpy2DAsync(h->dfbuf, (size_t)h->max_steps * 3 * sizeof(float), dL_dforce,
                                   (size_t)n * 3 * sizeof(float), (size_t)n * 3 * sizeof(float), (size_t)h->B,
                                   cudaMemcpyDeviceToDevice, st));
-    long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant, h->block * 4096 + h->gblock, 0, 0};
+    long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant * 16 + h->fuse * 2 + h->fuse_adj,
+                         h->block * 4096 + h->gblock, 0, 0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, [&](cudaStream_t s2) { enqueue_backward(h, s2); });
     if (rc) return rc;
@@ -857,6 +934,18 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         h->use_graph = value ? 1 : 0;
         return DSTIR_OK;
     }
+    if (!strcmp(key, "fuse_adj")) {
+        h->fuse_adj = value ? 1 : 0;
+        h->recorded = false;
+        ++h->epoch;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "fuse")) {
+        h->fuse = value ? 1 : 0;
+        h->recorded = false;
+        ++h->epoch;
+        return DSTIR_OK;
+    }
     if (!strcmp(key, "brick_scatter")) {
         if (value < 0 || value > 2) return fail(h, DSTIR_EINVAL, "brick_scatter %lld not in 0..2", (long long)value);
         h->brick_scatter = (int)value;
@@ -890,6 +979,8 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "graph")) *value = h->use_graph;
     else if (!strcmp(key, "brick_gather")) *value = h->brick_gather;
     else if (!strcmp(key, "brick_scatter")) *value = h->brick_scatter;
+    else if (!strcmp(key, "fuse")) *value = h->fuse;
+    else if (!strcmp(key, "fuse_adj")) *value = h->fuse_adj;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

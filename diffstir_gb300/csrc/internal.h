@@ -30,6 +30,9 @@ struct FwdArgs {
     unsigned* status;       // DSTIR_STATUS_* word
     int clear_pm;           // grid kernel zeroes pm after reading it
     int batch;
+    // fused G2P(f) + P2G(f+1) only: F of state f+2 and the grid of substep f+1
+    float* next2;
+    float4* pm_next;
 };
 
 struct AdjArgs {
@@ -56,6 +59,10 @@ struct AdjArgs {
     float* partial;
     unsigned* counters;
     int batch;
+    // fused P2G adjoint of substep f with the G2P adjoint of substep f-1 only
+    const float* cur2;       // state at substep f-1
+    const float4* vo2;       // grid velocity of substep f-1
+    float* adj_prev;         // adjoint slot of state f-1 (receives its position-adjoint part)
 };
 
 // Counting sort of the particles of one substep by stencil-base cell.
@@ -82,10 +89,15 @@ enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_CELL = 2, P2G_BRICK = 3 };
 void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st);
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st);
 void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st);
+// G2P of substep f (into a.next) fused with the stress and P2G scatter of
+// substep f+1 (F into a.next2, grid into a.pm_next)
+void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st);
 
 void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st);
 void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st);
 void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st);
+// P2G adjoint of substep f fused with the G2P adjoint of substep f-1
+void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st);
 
 void launch_bin(const BinArgs& b, int n_blocks, int block, cudaStream_t st);
 int bin_scan_blocks(long long G);

@@ -253,6 +253,156 @@ __global__ void __launch_bounds__(256) g2p_kernel(FwdArgs a) {
     }
 }
 
+// G2P of substep f fused with P2G of substep f+1 (one thread per particle).
+// The G2P half is g2p_kernel; its new x, v, C stay in registers for the
+// stress of substep f+1 (compute_F_tmp :39-42 with F[f+1] read back, p2g
+// :104-196), which scatters into the next grid.  Saves a pass over the
+// particle state and a launch per substep.
+template <int VARIANT, bool SVDJ>
+__global__ void __launch_bounds__(256) g2p_p2g_kernel(FwdArgs a) {
+    __shared__ SceneDev s;
+    __shared__ BlockInfo bi;
+    __shared__ float sh[32][4];
+    __shared__ float tv[3];
+    __shared__ float prm[4];
+    __shared__ int model;
+    if (threadIdx.x == 0) {
+        bi = a.blk[blockIdx.x];
+        s = a.sc[bi.scene];
+        const float* t0 = a.traj + ((long long)bi.scene * a.traj_len + a.f) * 3;
+        for (int c = 0; c < 3; ++c) tv[c] = (t0[3 + c] - t0[c]) / s.dt;
+        for (int i = 0; i < 4; ++i) prm[i] = a.params[bi.scene * 4 + i];
+        model = a.models[bi.scene];
+    }
+    __syncthreads();
+    long long p = bi.start + threadIdx.x;
+    bool active = p < bi.end;
+    float dv[3] = {0.f, 0.f, 0.f};
+    if (active) {
+        // ---- G2P of substep f
+        float x[3];
+        load3(a.cur, a.stride, OX, p, x);
+        int base[3];
+        float fx[3];
+        float nv[3] = {0.f, 0.f, 0.f}, nC[9];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) nC[i] = 0.f;
+        if (locate(x, s.inv_dx, s.n, base, fx)) {
+            float w[3][3];
+            bspline(fx, w);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    float wij = w[i][0] * w[j][1];
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        float4 g = __ldg(a.vo + row + k);
+                        float W = wij * w[k][2];
+                        float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
+                        float wg0 = W * g.x, wg1 = W * g.y, wg2 = W * g.z;
+                        nv[0] += wg0;
+                        nv[1] += wg1;
+                        nv[2] += wg2;
+                        nC[0] += wg0 * d0; nC[1] += wg0 * d1; nC[2] += wg0 * d2;
+                        nC[3] += wg1 * d0; nC[4] += wg1 * d1; nC[5] += wg1 * d2;
+                        nC[6] += wg2 * d0; nC[7] += wg2 * d1; nC[8] += wg2 * d2;
+                    }
+                }
+            float c4 = 4.f * s.inv_dx;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) nC[i] *= c4;
+        } else {
+            atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
+        }
+        float vn[3];
+        if (bi.kind == KIND_LIQUID) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                vn[c] = nv[c];
+                x[c] = x[c] + s.dt * nv[c];
+            }
+            bool fin = isfinite(x[0]) && isfinite(x[1]) && isfinite(x[2]) && isfinite(nv[0]) && isfinite(nv[1]) &&
+                       isfinite(nv[2]);
+#pragma unroll
+            for (int i = 0; i < 9; ++i) fin = fin && isfinite(nC[i]);
+            if (!fin) atomicOr(a.status, DSTIR_STATUS_NAN);
+        } else if (bi.kind == KIND_ROD) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                dv[c] = tv[c] - nv[c];
+                vn[c] = tv[c];
+                x[c] = x[c] + tv[c] * s.dt;
+            }
+        } else {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) vn[c] = 0.f;
+        }
+        store9(a.next, a.stride, OC, p, nC);
+        store3(a.next, a.stride, OV, p, vn);
+        store3(a.next, a.stride, OX, p, x);
+        // ---- P2G of substep f+1 from (x, vn, nC) and F[f+1]
+        float F[9];
+        load9(a.next, a.stride, OF, p, F);
+        float m, mv[3], A[9];
+        if (bi.kind == KIND_LIQUID) {
+            LiquidP2G q;
+            liquid_p2g<SVDJ>(s, model, prm, vn, nC, F, q);
+            store9(a.next2, a.stride, OF, p, q.Ft);
+            m = s.m_liq;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) A[i] = q.A[i];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) mv[c] = m * q.vv[c];
+        } else {
+            store9(a.next2, a.stride, OF, p, F);
+            m = (bi.kind == KIND_ROD) ? s.m_rod : s.m_cont;
+#pragma unroll
+            for (int i = 0; i < 9; ++i) A[i] = m * nC[i];
+#pragma unroll
+            for (int c = 0; c < 3; ++c) mv[c] = m * vn[c];
+        }
+        if (locate(x, s.inv_dx, s.n, base, fx)) {
+            float w[3][3];
+            bspline(fx, w);
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    float wij = w[i][0] * w[j][1];
+                    long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        float W = wij * w[k][2];
+                        float dp0 = ((float)i - fx[0]) * s.dx, dp1 = ((float)j - fx[1]) * s.dx,
+                              dp2 = ((float)k - fx[2]) * s.dx;
+                        float g0 = W * (mv[0] + (A[0] * dp0 + A[1] * dp1 + A[2] * dp2));
+                        float g1 = W * (mv[1] + (A[3] * dp0 + A[4] * dp1 + A[5] * dp2));
+                        float g2 = W * (mv[2] + (A[6] * dp0 + A[7] * dp1 + A[8] * dp2));
+                        float gm = W * m;
+                        float4* dst = a.pm_next + row + k;
+                        if (VARIANT == P2G_PLAIN) {
+                            float* d = reinterpret_cast<float*>(dst);
+                            atomicAdd(d + 0, g0);
+                            atomicAdd(d + 1, g1);
+                            atomicAdd(d + 2, g2);
+                            atomicAdd(d + 3, gm);
+                        } else {
+                            red_add4(dst, g0, g1, g2, gm);
+                        }
+                    }
+                }
+        } else {
+            atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
+        }
+    }
+    if (bi.kind == KIND_ROD && s.rod_mode == DSTIR_ROD_PARTICLES) {
+        group_sum<3>(dv, sh, a.partial, a.counters + a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,
+                     a.force + bi.scene * a.force_stride + (long long)a.fo * 3, s.force_scale);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // adjoint
 // ---------------------------------------------------------------------------
@@ -470,6 +620,137 @@ __global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
     }
 }
 
+// P2G adjoint of substep f fused with the G2P adjoint of substep f-1.  The
+// state adjoint of f (x, v, C parts) goes from the first half to the second
+// in registers; only its F part (read by the P2G adjoint of f-1) and the
+// position-adjoint part of f-1 are stored.
+template <int VARIANT, bool SVDJ>
+__global__ void __launch_bounds__(256) p2g_adj_g2p_adj_kernel(AdjArgs a) {
+    __shared__ SceneDev s;
+    __shared__ BlockInfo bi;
+    __shared__ float sh[32][4];
+    __shared__ float prm[4];
+    __shared__ int model;
+    __shared__ float fb[3];
+    if (threadIdx.x == 0) {
+        bi = a.blk[blockIdx.x];
+        s = a.sc[bi.scene];
+        for (int i = 0; i < 4; ++i) prm[i] = a.params[bi.scene * 4 + i];
+        model = a.models[bi.scene];
+        const float* d = a.dforce + bi.scene * a.dforce_stride + (long long)(a.fo - 1) * 3;
+        for (int c = 0; c < 3; ++c) fb[c] = d[c];
+    }
+    __syncthreads();
+    long long p = bi.start + threadIdx.x;
+    float pg[4] = {0.f, 0.f, 0.f, 0.f};
+    if (p < bi.end) {
+        const int kind = bi.kind;
+        const bool liquid = kind == KIND_LIQUID;
+        // ---- P2G adjoint of substep f
+        float xb[3], vb[3], Cb[9];
+        {
+            float x[3];
+            load3(a.cur, a.stride, OX, p, x);
+            float m, mv[3], A[9];
+            p2g_adj_affine<SVDJ>(a.cur, a.stride, s, prm, model, p, kind, m, mv, A);
+            float Ab[9], vvb[3] = {0.f, 0.f, 0.f}, fxb[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < 9; ++i) Ab[i] = 0.f;
+            int base[3];
+            float fx[3];
+            if (locate(x, s.inv_dx, s.n, base, fx)) {
+                float w[3][3], dw[3][3];
+                bspline_d(fx, w, dw);
+#pragma unroll
+                for (int i = 0; i < 3; ++i)
+#pragma unroll
+                    for (int j = 0; j < 3; ++j) {
+                        long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+#pragma unroll
+                        for (int k = 0; k < 3; ++k) {
+                            float dp[3] = {((float)i - fx[0]) * s.dx, ((float)j - fx[1]) * s.dx,
+                                           ((float)k - fx[2]) * s.dx};
+                            p2g_adj_node(w[i][0] * w[j][1] * w[k][2], dw[i][0] * w[j][1] * w[k][2],
+                                         w[i][0] * dw[j][1] * w[k][2], w[i][0] * w[j][1] * dw[k][2], dp,
+                                         __ldg(a.pmb + row + k), m, mv, A, s.dx, liquid, Ab, vvb, fxb);
+                        }
+                    }
+            }
+            float Fb[9];
+            p2g_adj_core<SVDJ>(a, s, prm, model, p, kind, m, Ab, vvb, fxb, pg, xb, vb, Cb, Fb);
+            store9(a.adj_cur, a.stride, OF, p, Fb);
+        }
+        // ---- G2P adjoint of substep f-1 (g2p_adj_kernel) with the adjoint of state f
+        float x[3];
+        load3(a.cur2, a.stride, OX, p, x);
+        float vnb[3], xbo[3] = {0.f, 0.f, 0.f};
+        if (liquid) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                vnb[c] = vb[c] + s.dt * xb[c];
+                xbo[c] = xb[c];
+            }
+        } else if (kind == KIND_ROD && s.rod_mode == DSTIR_ROD_PARTICLES) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) vnb[c] = -fb[c] * s.force_scale;
+        } else {
+            vnb[0] = vnb[1] = vnb[2] = 0.f;
+        }
+        int base[3];
+        float fx[3];
+        if (locate(x, s.inv_dx, s.n, base, fx)) {
+            float w[3][3], dw[3][3];
+            bspline_d(fx, w, dw);
+            const float c4 = 4.f * s.inv_dx;
+            float fxb[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+            for (int i = 0; i < 3; ++i)
+#pragma unroll
+                for (int j = 0; j < 3; ++j) {
+                    long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+#pragma unroll
+                    for (int k = 0; k < 3; ++k) {
+                        float W = w[i][0] * w[j][1] * w[k][2];
+                        float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
+                        float Cd0 = Cb[0] * d0 + Cb[1] * d1 + Cb[2] * d2;
+                        float Cd1 = Cb[3] * d0 + Cb[4] * d1 + Cb[5] * d2;
+                        float Cd2 = Cb[6] * d0 + Cb[7] * d1 + Cb[8] * d2;
+                        float4* dst = a.ga + row + k;
+                        float g0 = W * (vnb[0] + c4 * Cd0), g1 = W * (vnb[1] + c4 * Cd1),
+                              g2 = W * (vnb[2] + c4 * Cd2);
+                        if (VARIANT == P2G_PLAIN) {
+                            float* dd = reinterpret_cast<float*>(dst);
+                            atomicAdd(dd + 0, g0);
+                            atomicAdd(dd + 1, g1);
+                            atomicAdd(dd + 2, g2);
+                        } else {
+                            red_add4(dst, g0, g1, g2, 0.f);
+                        }
+                        if (liquid) {
+                            float4 g = __ldg(a.vo2 + row + k);
+                            float Wb = vnb[0] * g.x + vnb[1] * g.y + vnb[2] * g.z +
+                                       c4 * (g.x * Cd0 + g.y * Cd1 + g.z * Cd2);
+                            fxb[0] -= c4 * W * (Cb[0] * g.x + Cb[3] * g.y + Cb[6] * g.z);
+                            fxb[1] -= c4 * W * (Cb[1] * g.x + Cb[4] * g.y + Cb[7] * g.z);
+                            fxb[2] -= c4 * W * (Cb[2] * g.x + Cb[5] * g.y + Cb[8] * g.z);
+                            fxb[0] += Wb * dw[i][0] * w[j][1] * w[k][2];
+                            fxb[1] += Wb * w[i][0] * dw[j][1] * w[k][2];
+                            fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
+                        }
+                    }
+                }
+            if (liquid)
+#pragma unroll
+                for (int c = 0; c < 3; ++c) xbo[c] += s.inv_dx * fxb[c];
+        }
+        if (liquid) store3(a.adj_prev, a.stride, OX, p, xbo);
+    }
+    if (bi.kind == KIND_LIQUID) {
+        group_sum<4>(pg, sh, a.partial, a.counters + 2 * a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,
+                     a.pgrad + ((long long)a.fo * a.batch + bi.scene) * 4, 1.f);
+    }
+}
+
 // ---------------------------------------------------------------------------
 // layout and reduction helpers
 // ---------------------------------------------------------------------------
@@ -533,6 +814,15 @@ void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
 void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st) {
     if (n_blocks > 0) g2p_kernel<<<n_blocks, block, 0, st>>>(a);
 }
+void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st) {
+    if (n_blocks <= 0) return;
+    if (variant == P2G_PLAIN)
+        svdj ? g2p_p2g_kernel<P2G_PLAIN, true><<<n_blocks, block, 0, st>>>(a)
+             : g2p_p2g_kernel<P2G_PLAIN, false><<<n_blocks, block, 0, st>>>(a);
+    else
+        svdj ? g2p_p2g_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
+             : g2p_p2g_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
+}
 void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st) {
     if (n_blocks <= 0) return;
     if (variant == P2G_PLAIN)
@@ -549,6 +839,15 @@ void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaSt
         p2g_adj_kernel<true><<<n_blocks, block, 0, st>>>(a);
     else
         p2g_adj_kernel<false><<<n_blocks, block, 0, st>>>(a);
+}
+void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st) {
+    if (n_blocks <= 0) return;
+    if (variant == P2G_PLAIN)
+        svdj ? p2g_adj_g2p_adj_kernel<P2G_PLAIN, true><<<n_blocks, block, 0, st>>>(a)
+             : p2g_adj_g2p_adj_kernel<P2G_PLAIN, false><<<n_blocks, block, 0, st>>>(a);
+    else
+        svdj ? p2g_adj_g2p_adj_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
+             : p2g_adj_g2p_adj_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
                        long long stride, long long n, cudaStream_t s) {

@@ -334,24 +334,35 @@ CONFIGS = {
     # 64^3, 8 ppc, ~600k particles, 2000 substeps, checkpoint every 50
     'C2': dict(n_grid=64, ppc=8, lo=(0.1, 0.05, 0.1), hi=(0.9, 0.5, 0.9), dt=2e-4, n_steps=2000,
                params=None, rod_radius=0.03, path='circle', ckpt=50),
-    # 64^3 batched, fill height U[0.15, 0.45], 1000 substeps
+    # 64^3 batched, fill height U[0.15, 0.45], 1000 substeps.  n is drawn below 1:
+    # shear-thickening draws (n >= 1 with K ~ 1-2) exceed the explicit viscous
+    # limit at dt = 2e-4 on 64^3 and blow up within ~10 substeps, in the FP64
+    # CPU restatement as on the GPU.
     'C3': dict(n_grid=64, ppc=8, lo=(0.2, 0.05, 0.2), hi=(0.8, None, 0.8), dt=2e-4, n_steps=1000,
-               params=None, rod_radius=0.03, path='circle', ckpt=50, batch=64, yield_stress=True),
+               params=None, rod_radius=0.03, path='circle', ckpt=50, batch=64, yield_stress=True,
+               n_range=(0.4, 1.0)),
     # 128^3, 8 ppc, ~4.8M particles, 4000 substeps, r=0.02, sinusoid path
     'C4': dict(n_grid=128, ppc=8, lo=(0.1, 0.05, 0.1), hi=(0.9, 0.5, 0.9), dt=2e-4, n_steps=4000,
                params=None, rod_radius=0.02, path='sinusoids', ckpt=100),
     # 64^3, ~410k particles, 1500 substeps, identification with 16 restarts
     'C5': dict(n_grid=64, ppc=8, lo=(0.15, 0.05, 0.15), hi=(0.85, 0.45, 0.85), dt=2e-4,
                n_steps=1500, params=None, rod_radius=0.03, path='circle', ckpt=50, restarts=16,
-               yield_stress=True),
+               yield_stress=True, n_range=(0.4, 1.0)),
 }
 
 
-def draw_params(rng, yield_stress=False):
+def draw_params(rng, yield_stress=False, n_range=(0.4, 1.2)):
+    """(K, tau_y, n) of the synthetic workloads: K ~ U[0.1, 2], n ~ U[n_range],
+    tau_y ~ U[0, 5] (or 0).  Returned in the reference's parameter order
+    [K, tau_y, n, unused] (simulation_functions.py:138-146)."""
     K = rng.uniform(0.1, 2.0)
-    n = rng.uniform(0.4, 1.2)
+    n = rng.uniform(*n_range)
     tau = rng.uniform(0.0, 5.0) if yield_stress else 0.0
     return np.array([K, tau, n, 0.0])
+
+
+def config_n_range(name):
+    return CONFIGS[name].get('n_range', (0.4, 1.2))
 
 
 def synthetic_scene(name='C1', seed=0, n_steps=None, n_grid=None, fill_height=None, params=None,
@@ -368,7 +379,7 @@ def synthetic_scene(name='C1', seed=0, n_steps=None, n_grid=None, fill_height=No
     pos = block_particles(ng, cfg['ppc'], lo, hi, rng)
     if params is None:
         params = cfg['params'] if cfg['params'] is not None else draw_params(
-            rng, cfg.get('yield_stress', False))
+            rng, cfg.get('yield_stress', False), cfg.get('n_range', (0.4, 1.2)))
     if cfg['path'] == 'circle':
         traj = circle_trajectory(T, cfg['dt'])
     else:
