@@ -110,8 +110,8 @@ struct DstirHandle {
     int block = 256, gblock = 256, p2g_variant = P2G_VEC, use_graph = 0;
     int brick_gather = 1;   // with P2G_BRICK: G2P and the P2G adjoint also gather from brick tiles
     int brick_scatter = 1;  // with P2G_BRICK: 0 shared atomics, 1 shared red, 2 direct global atomics
-    int fuse = 1;           // per-particle variants: G2P(f) and P2G(f+1) in one kernel
-    int fuse_adj = 1;       // per-particle variants: P2G adjoint of f and G2P adjoint of f-1 in one kernel
+    int fuse = 0;           // per-particle variants: G2P(f) and P2G(f+1) in one kernel (measured 4% slower at 64^3)
+    int fuse_adj = 0;       // per-particle variants: P2G adjoint of f and G2P adjoint of f-1 in one kernel
     std::vector<BlockInfo> blk_h;
     std::vector<GridBlock> gblk_h;
     SceneDev* sc = nullptr;
@@ -610,15 +610,19 @@ bool fused_adj(const DstirHandle* h) { return h->fuse_adj && !binned(h); }
 // Forward chain of `nsteps` substeps over the state slots slot(0..nsteps).
 // With fusion: P2G(0), then per substep k the grid update and G2P(k) fused
 // with P2G(k+1); the last substep ends with a plain G2P unless `skip_last_g2p`.
+// `per_step_bins`: binned variants keep the bins of substep k in bin slot k
+// (the segment recompute, whose bins the reverse pass reuses); otherwise every
+// substep bins into slot 0 (a forward rollout owns a single bin slot).
 template <class SlotFn, class GridFn>
 void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids, float* force,
-                   long long fstride, int fo0, int clear_pm, bool skip_last_g2p, cudaStream_t st) {
+                   long long fstride, int fo0, int clear_pm, bool skip_last_g2p, bool per_step_bins,
+                   cudaStream_t st) {
     if (!fused(h)) {
         for (int k = 0; k < nsteps; ++k) {
             float4 *pm, *vo;
             grids(k, pm, vo);
             FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + k, force, fstride, fo0 + k, clear_pm);
-            run_substep(h, a, st, k);
+            run_substep(h, a, st, per_step_bins ? k : 0);
         }
         return;
     }
@@ -663,7 +667,7 @@ int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, cuda
         pm = h->pm;
         vo = h->vo;
     };
-    chain_forward(h, t0, nsteps, slot, grids, h->fbuf, (long long)h->max_steps * 3, 0, 1, false, st);
+    chain_forward(h, t0, nsteps, slot, grids, h->fbuf, (long long)h->max_steps * 3, 0, 1, false, false, st);
     return (cur + nsteps) % 3;
 }
 
@@ -799,7 +803,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
         // recompute the segment, keeping every state and grid; the state after
         // its last substep is not needed by the adjoint
         chain_forward(h, t0 + s0, L, slot, grids, h->force_scratch, (long long)h->max_steps * 3, t0 + s0, 0, true,
-                      st);
+                      true, st);
         // adjoint of the state at global step g (relative to t0) lives in A[(n - g) & 1]
         auto adj_args = [&](int k) {
             AdjArgs a;

@@ -64,8 +64,8 @@ def fixture_scene(name, model):
                  d['operator_trajectory'], d['m%d_params' % model]), d
 
 
-VARIANTS = [{'p2g': 1}, {'p2g': 1, 'fuse': 0, 'fuse_adj': 0}, {'p2g': 1, 'fuse': 1, 'fuse_adj': 0},
-            {'p2g': 0, 'graph': 1}, {'p2g': 2}, {'p2g': 3},
+VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse': 1, 'fuse_adj': 0},
+            {'p2g': 0, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 2}, {'p2g': 3},
             {'p2g': 3, 'brick_scatter': 0}, {'p2g': 3, 'brick_scatter': 2}, {'p2g': 3, 'brick_gather': 0},
             {'p2g': 3, 'graph': 1}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
