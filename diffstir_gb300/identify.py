@@ -159,6 +159,8 @@ def main(argv=None):
     ap.add_argument('--ckpt', type=int, default=None)
     ap.add_argument('--seed', type=int, default=0)
     ap.add_argument('--noise', type=float, default=0.01)
+    ap.add_argument('--plain-iters', type=int, default=2,
+                    help='iterations of the plain comparison: one restart alone, scalar atomics, no graph')
     args = ap.parse_args(argv)
     cfg = S.CONFIGS[args.config]
     T = args.substeps or cfg['n_steps']
@@ -175,6 +177,14 @@ def main(argv=None):
     bounds[2] = tuple(cfg.get('n_range', HB_BOUNDS[2]))   # stay inside the explicitly stable range
     res = adam_identify(sc, target, restarts=R, iters=args.iters, lr=args.lr, ckpt_every=args.ckpt or cfg['ckpt'],
                         free=free, bounds=bounds, seed=args.seed + 1)
+    res['sim'].close()
+    plain = None
+    if args.plain_iters > 0:
+        p1 = adam_identify(sc, target, restarts=1, iters=args.plain_iters, lr=args.lr,
+                           ckpt_every=args.ckpt or cfg['ckpt'], free=free, bounds=bounds, seed=args.seed + 1,
+                           options={'p2g': 0, 'graph': 0, 'fuse': 0, 'fuse_adj': 0})
+        p1['sim'].close()
+        plain = p1['grad_evals'] / p1['wall_s']
     best = res['best']
     rel = {name: float(abs(best[i] - truth[i]) / max(abs(truth[i]), 1e-12)) for name, i in
            (('K', 0), ('tau_y', 1), ('n', 2)) if i in free}
