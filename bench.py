@@ -79,6 +79,9 @@ def parse():
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')
     ap.add_argument('--no-cpu', action='store_true')
+    ap.add_argument('--no-fd', action='store_true', help='skip the central-difference gradient check')
+    ap.add_argument('--no-plain', action='store_true', help='skip the plain single-scene comparison')
+    ap.add_argument('--fd-h', type=float, default=1e-3, help='relative step of the gradient check')
     return ap.parse_args()
 
 
@@ -330,6 +333,82 @@ def run_ours(args):
         n_total = float(N)
     value = n_total * T / (ms / 1e3)
 
+    # forward-only rate: the same rollout without recording checkpoints
+    sim.set_params(params)
+    sim.reset()
+    sim.forward(T)
+    torch.cuda.synchronize()
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record(stream)
+    for _ in range(args.steps):
+        sim.reset()
+        sim.forward(T)
+    f1.record(stream)
+    torch.cuda.synchronize()
+    fwd_ms = f0.elapsed_time(f1) / args.steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([fwd_ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        fwd_ms = float(t.item())
+
+    # central differences of each scene's loss w.r.t. its free parameters, all
+    # scenes perturbed at once (they are independent), against the adjoint
+    grad_check = None
+    if not args.no_fd:
+        _, dp_adj = grad_eval(params)
+        free = [0, 1, 2] if ys else [0, 2]
+        names = {0: 'K', 1: 'tau_y', 2: 'n'}
+
+        def scene_losses(p):
+            sim.set_params(p)
+            sim.reset()
+            f = sim.forward(T)
+            diff = (f - target)[..., 0::2].double()
+            return (diff * diff).sum(dim=(1, 2)) / float(B * T * 2)
+
+        errs = {}
+        for i in free:
+            hs = args.fd_h * params[:, i].abs().clamp_min(1e-3)
+            pp, pm = params.clone(), params.clone()
+            pp[:, i] += hs
+            pm[:, i] -= hs
+            fd = (scene_losses(pp) - scene_losses(pm)) / (2.0 * hs.double())
+            ad = dp_adj[:, i].double()
+            errs[names[i]] = float(((ad - fd).abs() / fd.abs().clamp_min(1e-30)).max())
+        grad_check = {'method': 'central differences of each scene loss, h = %g x |param|' % args.fd_h,
+                      'rel_err_max': max(errs.values()), 'rel_err': errs, 'steps': T}
+
+    # plain comparison: one scene of the workload alone, per-particle scalar
+    # atomics, particles in generation order, no graph
+    plain = None
+    if not args.no_plain:
+        ps = Simulator([sc], max_steps=T, options={'p2g': 0, 'graph': 0, 'fuse': 0, 'fuse_adj': 0}, reorder=False)
+        tgt1 = target[:1].contiguous()
+        p1 = params[:1].contiguous()
+
+        def plain_eval():
+            ps.set_params(p1)
+            ps.reset()
+            f = ps.forward(T, ckpt_every=ckpt, record=True)
+            diff = (f - tgt1)[..., 0::2]
+            dF = torch.zeros_like(f)
+            dF[..., 0::2] = 2.0 * diff / diff.numel()
+            return ps.backward(dF)
+
+        plain_eval()
+        torch.cuda.synchronize()
+        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        q0.record(stream)
+        plain_eval()
+        q1.record(stream)
+        torch.cuda.synchronize()
+        pms = q0.elapsed_time(q1)
+        ps.close()
+        plain = {'grad_evals_per_s': 1e3 / pms, 'value': sc.n_particles * T / (pms / 1e3), 'unit': UNIT,
+                 'ms_per_grad_eval': pms,
+                 'what': 'scene 0 alone, scalar atomics, generation order, no graph, 1 timed gradient evaluation'}
+
     # e2e through the public API with pinned host inputs / host results
     e2e = None
     if not args.no_e2e:
@@ -408,6 +487,9 @@ def run_ours(args):
                    'l2': 'inputs larger than L2 (checkpoints + segment states ~%.1f GB per step)' %
                          ((T // ckpt + ckpt) * N * 96 / 1e9)},
         'grad_evals_per_s': world * B * 1e3 / ms,
+        'forward_value': n_total * T / (fwd_ms / 1e3),
+        'grad_check': grad_check,
+        'plain': plain,
         'forward_adjoint_roofline_frac': step_bytes / (ms / 1e3) / 1e9 / hbm,
         'roofline': roof,
         'kernel_time_share': kernel_share,

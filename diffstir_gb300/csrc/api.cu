@@ -397,7 +397,7 @@ void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st, int bin_
                                 h->G, st);
         });
     } else {
-        int var = h->p2g_variant == P2G_PLAIN ? P2G_PLAIN : P2G_VEC;
+        const int var = h->p2g_variant;  // P2G_PLAIN, P2G_VEC or P2G_WARP here
         timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st); });
     }
     timed(h, K_GRID_ADJ, st, [&] { launch_grid_adj(a, h->n_gblocks, h->gblock, st); });
@@ -842,7 +842,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             // grid adjoint and the P2G adjoint of k fused with the G2P adjoint of
             // k-1; the first substep of the segment ends with a plain P2G adjoint
             // that stores the whole state adjoint for the previous segment
-            const int var = h->p2g_variant == P2G_PLAIN ? P2G_PLAIN : P2G_VEC;
+            const int var = h->p2g_variant;  // P2G_PLAIN, P2G_VEC or P2G_WARP here
             {
                 AdjArgs a = adj_args(L - 1);
                 timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st); });
@@ -919,7 +919,7 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream) {
 int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     if (!h || !key) return DSTIR_EINVAL;
     if (!strcmp(key, "p2g")) {
-        if (value < 0 || value > 3) return fail(h, DSTIR_EINVAL, "p2g variant %lld not in 0..3", (long long)value);
+        if (value < 0 || value > 4) return fail(h, DSTIR_EINVAL, "p2g variant %lld not in 0..4", (long long)value);
         h->p2g_variant = (int)value;
         h->recorded = false;
         return DSTIR_OK;

@@ -83,8 +83,9 @@ struct BinArgs {
 };
 
 // p2g variants: scalar atomics per particle, vector atomics per particle,
-// binned one-thread-per-cell accumulation
-enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_CELL = 2, P2G_BRICK = 3 };
+// binned one-thread-per-cell accumulation, brick tiles in shared memory,
+// vector atomics after warp run aggregation of the k-consecutive stencil rows
+enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_CELL = 2, P2G_BRICK = 3, P2G_WARP = 4 };
 
 void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st);
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st);

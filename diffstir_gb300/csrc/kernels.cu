@@ -34,8 +34,11 @@ __global__ void __launch_bounds__(256) p2g_kernel(FwdArgs a) {
         s = a.sc[bi.scene];
     }
     __syncthreads();
+    constexpr bool WARP = VARIANT == P2G_WARP;
     long long p = bi.start + threadIdx.x;
-    if (p >= bi.end) return;
+    bool active = p < bi.end;
+    if (!WARP && !active) return;
+    if (!active) p = bi.end - 1;  // WARP: the lane computes a copy and scatters nothing
     float x[3], v[3], C[9];
     load3(a.cur, a.stride, OX, p, x);
     load3(a.cur, a.stride, OV, p, v);
@@ -48,7 +51,7 @@ __global__ void __launch_bounds__(256) p2g_kernel(FwdArgs a) {
         for (int i = 0; i < 4; ++i) prm[i] = __ldg(a.params + bi.scene * 4 + i);
         LiquidP2G q;
         liquid_p2g<SVDJ>(s, __ldg(a.models + bi.scene), prm, v, C, F, q);
-        store9(a.next, a.stride, OF, p, q.Ft);  // F[f+1] = F_tmp (:153)
+        if (active) store9(a.next, a.stride, OF, p, q.Ft);  // F[f+1] = F_tmp (:153)
         m = s.m_liq;
 #pragma unroll
         for (int i = 0; i < 9; ++i) A[i] = q.A[i];
@@ -57,7 +60,7 @@ __global__ void __launch_bounds__(256) p2g_kernel(FwdArgs a) {
     } else {
         float F[9];
         load9(a.cur, a.stride, OF, p, F);
-        store9(a.next, a.stride, OF, p, F);
+        if (active) store9(a.next, a.stride, OF, p, F);
         m = (bi.kind == KIND_ROD) ? s.m_rod : s.m_cont;
 #pragma unroll
         for (int i = 0; i < 9; ++i) A[i] = m * C[i];
@@ -67,18 +70,24 @@ __global__ void __launch_bounds__(256) p2g_kernel(FwdArgs a) {
     int base[3];
     float fx[3];
     if (!locate(x, s.inv_dx, s.n, base, fx)) {
-        atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
-        return;
+        if (active) atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
+        if (!WARP) return;
+        active = false;
+        base[0] = base[1] = base[2] = 0;
+        fx[0] = fx[1] = fx[2] = 1.f;
     }
     float w[3][3];
     bspline(fx, w);
     float mv[3] = {m * vv[0], m * vv[1], m * vv[2]};
+    RunAgg ra;
+    if (WARP) ra = run_agg_flags(active ? (base[0] * s.n + base[1]) * s.n + base[2] : run_agg_inactive_key());
 #pragma unroll
     for (int i = 0; i < 3; ++i)
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             float wij = w[i][0] * w[j][1];
             long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+            float4 c[3];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
                 float W = wij * w[k][2];
@@ -95,10 +104,13 @@ __global__ void __launch_bounds__(256) p2g_kernel(FwdArgs a) {
                     atomicAdd(d + 1, g1);
                     atomicAdd(d + 2, g2);
                     atomicAdd(d + 3, gm);
-                } else {
+                } else if (VARIANT == P2G_VEC) {
                     red_add4(dst, g0, g1, g2, gm);
+                } else {
+                    c[k] = make_float4(g0, g1, g2, gm);
                 }
             }
+            if (WARP) run_agg_scatter<4>(ra, a.pm + row, c[0], c[1], c[2], active);
         }
 }
 
@@ -418,8 +430,11 @@ __global__ void __launch_bounds__(256) g2p_adj_kernel(AdjArgs a) {
         for (int c = 0; c < 3; ++c) fb[c] = d[c];
     }
     __syncthreads();
+    constexpr bool WARP = VARIANT == P2G_WARP;
     long long p = bi.start + threadIdx.x;
-    if (p >= bi.end) return;
+    bool active = p < bi.end;
+    if (!WARP && !active) return;
+    if (!active) p = bi.end - 1;  // WARP: the lane computes a copy and scatters nothing
     float x[3];
     load3(a.cur, a.stride, OX, p, x);
     float xb[3] = {0.f, 0.f, 0.f}, vnb[3], Cb[9];
@@ -441,9 +456,17 @@ __global__ void __launch_bounds__(256) g2p_adj_kernel(AdjArgs a) {
     }
     int base[3];
     float fx[3];
-    if (locate(x, s.inv_dx, s.n, base, fx)) {
+    bool inside = locate(x, s.inv_dx, s.n, base, fx);
+    if (WARP && !inside) {
+        active = false;
+        base[0] = base[1] = base[2] = 0;
+        fx[0] = fx[1] = fx[2] = 1.f;
+    }
+    if (inside || WARP) {
         float w[3][3], dw[3][3];
         bspline_d(fx, w, dw);
+        RunAgg ra;
+        if (WARP) ra = run_agg_flags(active ? (base[0] * s.n + base[1]) * s.n + base[2] : run_agg_inactive_key());
         float c4 = 4.f * s.inv_dx;
         float fxb[3] = {0.f, 0.f, 0.f};
         const bool liquid = bi.kind == KIND_LIQUID;
@@ -452,6 +475,7 @@ __global__ void __launch_bounds__(256) g2p_adj_kernel(AdjArgs a) {
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
                 long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                float4 cw[3];
 #pragma unroll
                 for (int k = 0; k < 3; ++k) {
                     float W = w[i][0] * w[j][1] * w[k][2];
@@ -466,8 +490,10 @@ __global__ void __launch_bounds__(256) g2p_adj_kernel(AdjArgs a) {
                         atomicAdd(dd + 0, g0);
                         atomicAdd(dd + 1, g1);
                         atomicAdd(dd + 2, g2);
-                    } else {
+                    } else if (VARIANT == P2G_VEC) {
                         red_add4(dst, g0, g1, g2, 0.f);
+                    } else {
+                        cw[k] = make_float4(g0, g1, g2, 0.f);
                     }
                     if (liquid) {
                         float4 g = __ldg(a.vo + row + k);
@@ -482,12 +508,13 @@ __global__ void __launch_bounds__(256) g2p_adj_kernel(AdjArgs a) {
                         fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
                     }
                 }
+                if (WARP) run_agg_scatter<3>(ra, a.ga + row, cw[0], cw[1], cw[2], active);
             }
         if (liquid)
 #pragma unroll
             for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
     }
-    if (bi.kind == KIND_LIQUID) store3(a.adj_cur, a.stride, OX, p, xb);
+    if (bi.kind == KIND_LIQUID && active) store3(a.adj_cur, a.stride, OX, p, xb);
 }
 
 __global__ void __launch_bounds__(256) grid_adj_kernel(AdjArgs a) {
@@ -804,6 +831,9 @@ void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svd
     if (variant == P2G_PLAIN)
         svdj ? p2g_kernel<P2G_PLAIN, true><<<n_blocks, block, 0, st>>>(a)
              : p2g_kernel<P2G_PLAIN, false><<<n_blocks, block, 0, st>>>(a);
+    else if (variant == P2G_WARP)
+        svdj ? p2g_kernel<P2G_WARP, true><<<n_blocks, block, 0, st>>>(a)
+             : p2g_kernel<P2G_WARP, false><<<n_blocks, block, 0, st>>>(a);
     else
         svdj ? p2g_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
              : p2g_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
@@ -827,6 +857,8 @@ void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cuda
     if (n_blocks <= 0) return;
     if (variant == P2G_PLAIN)
         g2p_adj_kernel<P2G_PLAIN><<<n_blocks, block, 0, st>>>(a);
+    else if (variant == P2G_WARP)
+        g2p_adj_kernel<P2G_WARP><<<n_blocks, block, 0, st>>>(a);
     else
         g2p_adj_kernel<P2G_VEC><<<n_blocks, block, 0, st>>>(a);
 }

@@ -192,7 +192,8 @@ def main(argv=None):
            'truth': truth.tolist(), 'best': best.tolist(), 'rel_err': rel,
            'best_loss': float(res['best_loss'].min()), 'initial_loss_min': float(res['history'][0].min()),
            'wall_s': res['wall_s'], 'grad_evals': res['grad_evals'],
-           'grad_evals_per_s': res['grad_evals'] / res['wall_s']}
+           'grad_evals_per_s': res['grad_evals'] / res['wall_s'], 'plain_grad_evals_per_s': plain,
+           'speedup_vs_plain': None if not plain else res['grad_evals'] / res['wall_s'] / plain}
     print(json.dumps(out), flush=True)
     return out
 

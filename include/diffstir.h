@@ -140,12 +140,17 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
 
 /* Tuning knobs: "p2g" (0 scalar atomics per particle, 1 vector atomics per
  * particle, 2 cell-binned one-thread-per-cell accumulation, 3 brick-binned
- * shared-memory tiles with one CTA per 4x4x4-cell brick; 2 and 3 also select
- * the matching G2P-adjoint scatter), "block" / "gblock" (threads per particle /
- * grid block: 64, 128 or 256), "graph" (1: replay each rollout and each
- * reverse pass as a cached CUDA graph), "profile" (1: time every launch with
- * CUDA events; totals via dstir_get_option "prof_ns:<kernel>" /
- * "prof_count:<kernel>"), "launches" (reset the launch counter). */
+ * shared-memory tiles with one CTA per 4x4x4-cell brick, 4 vector atomics
+ * after summing neighbouring lanes' contributions to shared stencil nodes by
+ * warp shuffles; 2, 3 and 4 also select the matching G2P-adjoint scatter),
+ * "block" / "gblock" (threads per particle / grid block: 64, 128 or 256),
+ * "graph" (1: replay each rollout and each reverse pass as a cached CUDA
+ * graph), "fuse" / "fuse_adj" (1: G2P of substep f fused with P2G of f+1 /
+ * P2G adjoint of f fused with the G2P adjoint of f-1), "brick_scatter" /
+ * "brick_gather" (scatter and gather forms of variant 3), "profile" (1: time
+ * every launch with CUDA events; totals via dstir_get_option
+ * "prof_ns:<kernel>" / "prof_count:<kernel>"), "launches" (reset the launch
+ * counter). */
 int dstir_set_option(DstirHandle* h, const char* key, int64_t value);
 int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value);
 

@@ -38,7 +38,7 @@ def rel(a, b):
 
 
 @pytest.mark.parametrize('config,T', [('C2', 6), ('C4', 3)])
-@pytest.mark.parametrize('opts', [{'p2g': 1}, {'p2g': 3}], ids=['vec', 'brick'])
+@pytest.mark.parametrize('opts', [{'p2g': 1}, {'p2g': 3}, {'p2g': 4}], ids=['vec', 'brick', 'warp'])
 def test_full_size_force_and_gradient(config, T, opts):
     sc = rounded(S.synthetic_scene(config, seed=0, n_steps=T))
     wts = np.random.default_rng(0).normal(size=(T, 3))

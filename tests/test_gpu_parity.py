@@ -67,9 +67,9 @@ def fixture_scene(name, model):
 VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse': 1, 'fuse_adj': 0},
             {'p2g': 0, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 2}, {'p2g': 3},
             {'p2g': 3, 'brick_scatter': 0}, {'p2g': 3, 'brick_scatter': 2}, {'p2g': 3, 'brick_gather': 0},
-            {'p2g': 3, 'graph': 1}]
+            {'p2g': 3, 'graph': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
-               'brick-global', 'brick-nogather', 'brick-graph']
+               'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
