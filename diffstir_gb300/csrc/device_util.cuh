@@ -81,22 +81,22 @@ __device__ __forceinline__ void red_add4(float4* p, float a, float b, float c, f
 // base node, row (i, j) of the stencil covers nodes key+o(i,j)+{0,1,2}, with
 // the same o(i,j) for every particle of the scene.  In the interleaved
 // particle order a warp holds particles of consecutive base cells of one grid
-// row, whose rows overlap their neighbours' by two nodes.  Contributions to a
-// node are then summed across lanes by shuffles before the vector RED:
-//   a1: lane L-1 has key-1, so its k+1 value lands on this lane's k+0 node;
-//   a2: lane L-2 has key-2, so its k+2 value lands on this lane's k+0 node;
-//   a lane takes lane L-1's k+2 value into its own k+1 value when a1 holds
-//   and lane L+1 does not take that k+1 value in turn.
-// Every value goes to exactly one lane (its own, or the lane whose k+0 or k+1
-// node it lands on), whatever the keys, so the sums are exact for any
-// particle order; only the number of REDs depends on it.  Inactive lanes take
-// distinct negative keys and zero values.  All 32 lanes must call these.
+// row, whose rows overlap their neighbours' by two nodes.  When lane L-1 has
+// key-1 (flag a1), two shuffle steps sum the overlapping values before the
+// vector RED:
+//   1. lane L adds lane L-1's k+2 value into its own k+1 value;
+//   2. lane L adds lane L-1's k+1 value (as updated by step 1) into its k+0.
+// A lane whose k+1 and k+2 values were taken by lane L+1 (n1) emits only its
+// k+0 value.  Every value reaches exactly one RED, whatever the keys, so the
+// sums are exact for any particle order; only the number of REDs depends on
+// it (34 instead of 96 per row for a warp on 32 consecutive base cells).
+// Inactive lanes take distinct negative keys and zero values.  All 32 lanes
+// must call these.
 // ---------------------------------------------------------------------------
 struct RunAgg {
-    bool a1, a2;   // take lane-1's k+1 / lane-2's k+2 value into k+0
-    bool e1, e2;   // this lane emits its k+1 / k+2 value
-    bool t1;       // take lane-1's k+2 value into k+1
-    bool any;      // some lane of the warp aggregates
+    bool a1;    // lane L-1 has key-1: take its k+1 and k+2 values
+    bool n1;    // lane L+1 takes this lane's k+1 and k+2 values
+    bool any;   // some lane of the warp aggregates
 };
 
 __device__ __forceinline__ int run_agg_inactive_key() { return -(1 << 29) - 4 * (int)(threadIdx.x & 31); }
@@ -104,50 +104,49 @@ __device__ __forceinline__ int run_agg_inactive_key() { return -(1 << 29) - 4 * 
 __device__ __forceinline__ RunAgg run_agg_flags(int key) {
     const unsigned full = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    int k1 = __shfl_up_sync(full, key, 1), k2 = __shfl_up_sync(full, key, 2);
+    int k1 = __shfl_up_sync(full, key, 1);
     RunAgg r;
     r.a1 = lane >= 1 && k1 == key - 1;
-    r.a2 = lane >= 2 && k2 == key - 2;
-    bool n1 = __shfl_down_sync(full, (int)r.a1, 1) && lane < 31;   // lane+1 takes my k+1
-    bool n2 = __shfl_down_sync(full, (int)r.a2, 2) && lane < 30;   // lane+2 takes my k+2
-    r.e1 = !n1;
-    r.e2 = !n1 && !n2;            // with n1 and not n2, lane+1 takes my k+2 into its k+1
-    r.t1 = r.a1 && !n1;
-    r.any = __any_sync(full, r.a1 || r.a2);
+    r.n1 = __shfl_down_sync(full, (int)r.a1, 1) && lane < 31;
+    r.any = __any_sync(full, r.a1);
     return r;
 }
 
-__device__ __forceinline__ float4 shfl_up4(float4 v, int d) {
-    const unsigned full = 0xffffffffu;
-    return make_float4(__shfl_up_sync(full, v.x, d), __shfl_up_sync(full, v.y, d), __shfl_up_sync(full, v.z, d),
-                       __shfl_up_sync(full, v.w, d));
-}
-
-__device__ __forceinline__ void add4(float4& a, const float4& b) {
-    a.x += b.x;
-    a.y += b.y;
-    a.z += b.z;
-    a.w += b.w;
-}
-
 // Aggregates one stencil row (c0, c1, c2 at nodes row+0..2) across the warp
-// and issues this lane's REDs.  NW: number of float components to add (3 or 4).
+// and issues this lane's REDs.  NW: float components carried (3 or 4; with 3
+// the w component is neither shuffled nor accumulated).
 template <int NW>
 __device__ __forceinline__ void run_agg_scatter(const RunAgg& r, float4* row, float4 c0, float4 c1, float4 c2,
                                                 bool active) {
+    const unsigned full = 0xffffffffu;
     if (r.any) {
-        float4 u1 = shfl_up4(c1, 1), v1 = shfl_up4(c2, 1), v2 = shfl_up4(c2, 2);
-        if (r.a1) add4(c0, u1);
-        if (r.a2) add4(c0, v2);
-        if (r.t1) add4(c1, v1);
+        float t0 = __shfl_up_sync(full, c2.x, 1), t1 = __shfl_up_sync(full, c2.y, 1),
+              t2 = __shfl_up_sync(full, c2.z, 1);
+        float t3 = NW == 4 ? __shfl_up_sync(full, c2.w, 1) : 0.f;
+        if (r.a1) {
+            c1.x += t0;
+            c1.y += t1;
+            c1.z += t2;
+            if (NW == 4) c1.w += t3;
+        }
+        t0 = __shfl_up_sync(full, c1.x, 1);
+        t1 = __shfl_up_sync(full, c1.y, 1);
+        t2 = __shfl_up_sync(full, c1.z, 1);
+        t3 = NW == 4 ? __shfl_up_sync(full, c1.w, 1) : 0.f;
+        if (r.a1) {
+            c0.x += t0;
+            c0.y += t1;
+            c0.z += t2;
+            if (NW == 4) c0.w += t3;
+        }
     }
     if (!active) return;
-    if (NW == 3) {
-        c0.w = c1.w = c2.w = 0.f;
-    }
+    if (NW == 3) c0.w = c1.w = c2.w = 0.f;
     atomicAdd(row, c0);
-    if (!r.any || r.e1) atomicAdd(row + 1, c1);
-    if (!r.any || r.e2) atomicAdd(row + 2, c2);
+    if (!r.n1) {
+        atomicAdd(row + 1, c1);
+        atomicAdd(row + 2, c2);
+    }
 }
 
 // ---------------------------------------------------------------------------

@@ -287,10 +287,12 @@ __global__ void __launch_bounds__(256) g2p_p2g_kernel(FwdArgs a) {
         model = a.models[bi.scene];
     }
     __syncthreads();
+    constexpr bool WARP = VARIANT == P2G_WARP;
     long long p = bi.start + threadIdx.x;
     bool active = p < bi.end;
+    if (WARP && !active) p = bi.end - 1;  // the lane computes a copy and writes nothing
     float dv[3] = {0.f, 0.f, 0.f};
-    if (active) {
+    if (active || WARP) {
         // ---- G2P of substep f
         float x[3];
         load3(a.cur, a.stride, OX, p, x);
@@ -325,7 +327,7 @@ __global__ void __launch_bounds__(256) g2p_p2g_kernel(FwdArgs a) {
             float c4 = 4.f * s.inv_dx;
 #pragma unroll
             for (int i = 0; i < 9; ++i) nC[i] *= c4;
-        } else {
+        } else if (active) {
             atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
         }
         float vn[3];
@@ -339,11 +341,11 @@ __global__ void __launch_bounds__(256) g2p_p2g_kernel(FwdArgs a) {
                        isfinite(nv[2]);
 #pragma unroll
             for (int i = 0; i < 9; ++i) fin = fin && isfinite(nC[i]);
-            if (!fin) atomicOr(a.status, DSTIR_STATUS_NAN);
+            if (!fin && active) atomicOr(a.status, DSTIR_STATUS_NAN);
         } else if (bi.kind == KIND_ROD) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
-                dv[c] = tv[c] - nv[c];
+                dv[c] = active ? tv[c] - nv[c] : 0.f;
                 vn[c] = tv[c];
                 x[c] = x[c] + tv[c] * s.dt;
             }
@@ -351,39 +353,51 @@ __global__ void __launch_bounds__(256) g2p_p2g_kernel(FwdArgs a) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) vn[c] = 0.f;
         }
-        store9(a.next, a.stride, OC, p, nC);
-        store3(a.next, a.stride, OV, p, vn);
-        store3(a.next, a.stride, OX, p, x);
         // ---- P2G of substep f+1 from (x, vn, nC) and F[f+1]
         float F[9];
         load9(a.next, a.stride, OF, p, F);
+        if (active) {
+            store9(a.next, a.stride, OC, p, nC);
+            store3(a.next, a.stride, OV, p, vn);
+            store3(a.next, a.stride, OX, p, x);
+        }
         float m, mv[3], A[9];
         if (bi.kind == KIND_LIQUID) {
             LiquidP2G q;
             liquid_p2g<SVDJ>(s, model, prm, vn, nC, F, q);
-            store9(a.next2, a.stride, OF, p, q.Ft);
+            if (active) store9(a.next2, a.stride, OF, p, q.Ft);
             m = s.m_liq;
 #pragma unroll
             for (int i = 0; i < 9; ++i) A[i] = q.A[i];
 #pragma unroll
             for (int c = 0; c < 3; ++c) mv[c] = m * q.vv[c];
         } else {
-            store9(a.next2, a.stride, OF, p, F);
+            if (active) store9(a.next2, a.stride, OF, p, F);
             m = (bi.kind == KIND_ROD) ? s.m_rod : s.m_cont;
 #pragma unroll
             for (int i = 0; i < 9; ++i) A[i] = m * nC[i];
 #pragma unroll
             for (int c = 0; c < 3; ++c) mv[c] = m * vn[c];
         }
-        if (locate(x, s.inv_dx, s.n, base, fx)) {
+        bool in2 = locate(x, s.inv_dx, s.n, base, fx);
+        if (!in2 && active) atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
+        bool act2 = active && in2;
+        if (WARP && !in2) {
+            base[0] = base[1] = base[2] = 0;
+            fx[0] = fx[1] = fx[2] = 1.f;
+        }
+        if (in2 || WARP) {
             float w[3][3];
             bspline(fx, w);
+            RunAgg ra;
+            if (WARP) ra = run_agg_flags(act2 ? (base[0] * s.n + base[1]) * s.n + base[2] : run_agg_inactive_key());
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
                     float wij = w[i][0] * w[j][1];
                     long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    float4 c[3];
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
                         float W = wij * w[k][2];
@@ -400,13 +414,14 @@ __global__ void __launch_bounds__(256) g2p_p2g_kernel(FwdArgs a) {
                             atomicAdd(d + 1, g1);
                             atomicAdd(d + 2, g2);
                             atomicAdd(d + 3, gm);
-                        } else {
+                        } else if (VARIANT == P2G_VEC) {
                             red_add4(dst, g0, g1, g2, gm);
+                        } else {
+                            c[k] = make_float4(g0, g1, g2, gm);
                         }
                     }
+                    if (WARP) run_agg_scatter<4>(ra, a.pm_next + row, c[0], c[1], c[2], act2);
                 }
-        } else {
-            atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
         }
     }
     if (bi.kind == KIND_ROD && s.rod_mode == DSTIR_ROD_PARTICLES) {
@@ -668,9 +683,12 @@ __global__ void __launch_bounds__(256) p2g_adj_g2p_adj_kernel(AdjArgs a) {
         for (int c = 0; c < 3; ++c) fb[c] = d[c];
     }
     __syncthreads();
+    constexpr bool WARP = VARIANT == P2G_WARP;
     long long p = bi.start + threadIdx.x;
+    const bool active = p < bi.end;
+    if (WARP && !active) p = bi.end - 1;  // the lane computes a copy and writes nothing
     float pg[4] = {0.f, 0.f, 0.f, 0.f};
-    if (p < bi.end) {
+    if (active || WARP) {
         const int kind = bi.kind;
         const bool liquid = kind == KIND_LIQUID;
         // ---- P2G adjoint of substep f
@@ -705,7 +723,12 @@ __global__ void __launch_bounds__(256) p2g_adj_g2p_adj_kernel(AdjArgs a) {
             }
             float Fb[9];
             p2g_adj_core<SVDJ>(a, s, prm, model, p, kind, m, Ab, vvb, fxb, pg, xb, vb, Cb, Fb);
-            store9(a.adj_cur, a.stride, OF, p, Fb);
+            if (active) {
+                store9(a.adj_cur, a.stride, OF, p, Fb);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 4; ++i) pg[i] = 0.f;
+            }
         }
         // ---- G2P adjoint of substep f-1 (g2p_adj_kernel) with the adjoint of state f
         float x[3];
@@ -725,16 +748,25 @@ __global__ void __launch_bounds__(256) p2g_adj_g2p_adj_kernel(AdjArgs a) {
         }
         int base[3];
         float fx[3];
-        if (locate(x, s.inv_dx, s.n, base, fx)) {
+        const bool in2 = locate(x, s.inv_dx, s.n, base, fx);
+        const bool act2 = active && in2;
+        if (WARP && !in2) {
+            base[0] = base[1] = base[2] = 0;
+            fx[0] = fx[1] = fx[2] = 1.f;
+        }
+        if (in2 || WARP) {
             float w[3][3], dw[3][3];
             bspline_d(fx, w, dw);
             const float c4 = 4.f * s.inv_dx;
             float fxb[3] = {0.f, 0.f, 0.f};
+            RunAgg ra;
+            if (WARP) ra = run_agg_flags(act2 ? (base[0] * s.n + base[1]) * s.n + base[2] : run_agg_inactive_key());
 #pragma unroll
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
                     long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    float4 cw[3];
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
                         float W = w[i][0] * w[j][1] * w[k][2];
@@ -750,8 +782,10 @@ __global__ void __launch_bounds__(256) p2g_adj_g2p_adj_kernel(AdjArgs a) {
                             atomicAdd(dd + 0, g0);
                             atomicAdd(dd + 1, g1);
                             atomicAdd(dd + 2, g2);
-                        } else {
+                        } else if (VARIANT == P2G_VEC) {
                             red_add4(dst, g0, g1, g2, 0.f);
+                        } else {
+                            cw[k] = make_float4(g0, g1, g2, 0.f);
                         }
                         if (liquid) {
                             float4 g = __ldg(a.vo2 + row + k);
@@ -765,12 +799,13 @@ __global__ void __launch_bounds__(256) p2g_adj_g2p_adj_kernel(AdjArgs a) {
                             fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
                         }
                     }
+                    if (WARP) run_agg_scatter<3>(ra, a.ga + row, cw[0], cw[1], cw[2], act2);
                 }
             if (liquid)
 #pragma unroll
                 for (int c = 0; c < 3; ++c) xbo[c] += s.inv_dx * fxb[c];
         }
-        if (liquid) store3(a.adj_prev, a.stride, OX, p, xbo);
+        if (liquid && active) store3(a.adj_prev, a.stride, OX, p, xbo);
     }
     if (bi.kind == KIND_LIQUID) {
         group_sum<4>(pg, sh, a.partial, a.counters + 2 * a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,
@@ -849,6 +884,9 @@ void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool
     if (variant == P2G_PLAIN)
         svdj ? g2p_p2g_kernel<P2G_PLAIN, true><<<n_blocks, block, 0, st>>>(a)
              : g2p_p2g_kernel<P2G_PLAIN, false><<<n_blocks, block, 0, st>>>(a);
+    else if (variant == P2G_WARP)
+        svdj ? g2p_p2g_kernel<P2G_WARP, true><<<n_blocks, block, 0, st>>>(a)
+             : g2p_p2g_kernel<P2G_WARP, false><<<n_blocks, block, 0, st>>>(a);
     else
         svdj ? g2p_p2g_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
              : g2p_p2g_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
@@ -877,6 +915,9 @@ void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int varia
     if (variant == P2G_PLAIN)
         svdj ? p2g_adj_g2p_adj_kernel<P2G_PLAIN, true><<<n_blocks, block, 0, st>>>(a)
              : p2g_adj_g2p_adj_kernel<P2G_PLAIN, false><<<n_blocks, block, 0, st>>>(a);
+    else if (variant == P2G_WARP)
+        svdj ? p2g_adj_g2p_adj_kernel<P2G_WARP, true><<<n_blocks, block, 0, st>>>(a)
+             : p2g_adj_g2p_adj_kernel<P2G_WARP, false><<<n_blocks, block, 0, st>>>(a);
     else
         svdj ? p2g_adj_g2p_adj_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
              : p2g_adj_g2p_adj_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
