@@ -29,26 +29,37 @@ def force_mse(force, target):
 
 
 def adam_identify(scene, target, restarts=16, iters=200, lr=1e-2, ckpt_every=50, free=(0, 1, 2), bounds=None,
-                  seed=0, options=None, log_every=0, callback=None):
+                  seed=0, options=None, log_every=0, callback=None, state0=None, init_params=None):
     """Fit the parameters ``free`` of ``scene`` to ``target`` [T,3] (or [1,T,3]).
 
     Parameters are optimised in normalised form u in [0,1] (p = lo + u (hi-lo))
-    with torch.optim.Adam(lr), clamped to the box after each step.  Returns a
-    dict with the best parameters per restart, the overall best, the loss
-    history [iters, R] and the wall time."""
+    with torch.optim.Adam(lr), clamped to the box after each step.  Restart 0
+    starts from ``init_params`` when given, the others from seeded uniform
+    draws.  ``state0`` (dict of x [n,3] and optionally v, C, F of one scene)
+    replaces the scene's step-0 state.  Returns a dict with the best
+    parameters per restart, the overall best, the loss history [iters, R] and
+    the wall time."""
     bounds = dict(HB_BOUNDS if bounds is None else bounds)
     T = scene.n_steps
     R = int(restarts)
     scenes = [copy.copy(scene) for _ in range(R)]
     sim = Simulator(scenes, max_steps=T, options=options)
     dev = sim.device
+    if state0 is not None:
+        tile = {k: None if state0.get(k) is None else
+                torch.as_tensor(state0[k], dtype=torch.float32, device=dev).reshape(scene.n_particles, -1).repeat(R, 1)
+                for k in ('x', 'v', 'C', 'F')}
+        sim.set_initial_state(tile['x'], tile['v'], tile['C'], tile['F'])
     tgt = torch.as_tensor(np.asarray(target), dtype=torch.float32, device=dev).reshape(1, T, 3).expand(R, T, 3)
     rng = np.random.default_rng(seed)
     free = list(free)
     lo = torch.tensor([bounds[i][0] for i in free], device=dev)
     hi = torch.tensor([bounds[i][1] for i in free], device=dev)
-    u = torch.tensor(rng.uniform(0.05, 0.95, size=(R, len(free))), dtype=torch.float32, device=dev,
-                     requires_grad=True)
+    u0 = rng.uniform(0.05, 0.95, size=(R, len(free)))
+    if init_params is not None:
+        ip = np.asarray(init_params, dtype=np.float64)
+        u0[0] = [np.clip((ip[i] - bounds[i][0]) / (bounds[i][1] - bounds[i][0]), 0.0, 1.0) for i in free]
+    u = torch.tensor(u0, dtype=torch.float32, device=dev, requires_grad=True)
     base = torch.as_tensor(np.asarray(scene.params), dtype=torch.float32, device=dev).reshape(1, 4).repeat(R, 1)
     opt = torch.optim.Adam([u], lr=lr)
     hist = np.zeros((iters, R))
@@ -82,6 +93,65 @@ def adam_identify(scene, target, restarts=16, iters=200, lr=1e-2, ckpt_every=50,
     k = int(np.argmin(best_loss))
     return {'best_params': bp, 'best_loss': best_loss, 'best': bp[k], 'best_index': k, 'history': hist,
             'wall_s': wall, 'grad_evals': iters * R, 'sim': sim}
+
+
+def clip_identify(scene, target, frames_per_clip, n_clips=None, carry='x', restarts=8, iters=50, lr=1e-2,
+                  ckpt_every=50, free=(0, 1, 2), bounds=None, seed=0, options=None, first_clip_factor=3,
+                  log_every=0):
+    """Clip-wise identification over a long trajectory, with the state carried
+    from clip to clip (the clip loop of src/gradient_descent_module.py:84-139).
+
+    Clip c covers substeps [c*frames_per_clip, (c+1)*frames_per_clip) of
+    ``scene.trajectory`` and of ``target`` [T,3].  Each clip is fitted by
+    :func:`adam_identify` (restart 0 continues from the previous clip's best
+    parameters; the first clip gets ``first_clip_factor`` times the
+    iterations, as the reference gives its first clip three times the epochs),
+    then rolled forward once with its best parameters to produce the next
+    clip's initial state.  ``carry='x'`` carries positions only and restarts
+    v, C, F from rest, as the reference does (initial_x.from_numpy of the last
+    frame, then initialize_ti_field); ``carry='full'`` carries x, v, C and F.
+    Two defects of the reference loop are not reproduced: its ``return`` sits
+    inside the clip loop (only clip 0 ever runs), and it loads the window of
+    the clip it just finished instead of the next one.
+
+    Returns a list with one dict per clip (best parameters, best loss, wall
+    time, loss history)."""
+    from .scene import Scene
+    T_all = min(scene.n_steps, np.asarray(target).shape[-2])
+    fpc = int(frames_per_clip)
+    if n_clips is None:
+        n_clips = T_all // fpc
+    target = np.asarray(target, dtype=np.float64).reshape(-1, 3)
+    state = None
+    params = None
+    out = []
+    for c in range(n_clips):
+        t0, t1 = c * fpc, (c + 1) * fpc
+        if t1 > T_all:
+            break
+        sub = Scene(scene.desc, scene.liquid_x, scene.rod_x, scene.container_x, scene.trajectory[t0:t1 + 1],
+                    scene.params if params is None else params, dict(scene.info))
+        res = adam_identify(sub, target[t0:t1], restarts=restarts,
+                            iters=iters * (first_clip_factor if c == 0 else 1), lr=lr, ckpt_every=ckpt_every,
+                            free=free, bounds=bounds, seed=seed + c, options=options, state0=state,
+                            init_params=params, log_every=log_every)
+        res['sim'].close()
+        params = res['best']
+        # roll the clip forward with its best parameters for the next initial state
+        sim = Simulator(sub, max_steps=fpc, options=options)
+        if state is not None:
+            sim.set_initial_state(state['x'], state.get('v'), state.get('C'), state.get('F'))
+        sim.set_params(torch.as_tensor(params, dtype=torch.float32).reshape(1, 4))
+        sim.forward(fpc)
+        st = sim.get_state()
+        n = scene.n_particles
+        state = {'x': st['x']} if carry == 'x' else {'x': st['x'], 'v': st['v'], 'C': st['C'].reshape(n, 9),
+                                                      'F': st['F'].reshape(n, 9)}
+        status = sim.status()
+        sim.close()
+        out.append({'clip': c, 'substeps': (t0, t1), 'best': params.copy(), 'best_loss': float(res['best_loss'].min()),
+                    'wall_s': res['wall_s'], 'history': res['history'], 'status': status})
+    return out
 
 
 # ---------------------------------------------------------------------------

@@ -116,6 +116,17 @@ class Simulator:
     def set_x0(self, x0):
         """Step-0 positions (caller order) used by :meth:`reset`; resets."""
         self._x0 = self._to_internal(x0, (self.N, 3))
+        self._init = (self._x0, None, None, None)
+        self.reset()
+
+    def set_initial_state(self, x, v=None, C=None, F=None):
+        """State (caller order) that :meth:`reset` restores from now on, for a
+        rollout that continues an earlier one (the next clip of a long
+        trajectory); v/C default to zero and F to identity, as in
+        :meth:`set_state`.  Resets."""
+        self._x0 = self._to_internal(x, (self.N, 3))
+        self._init = (self._x0, self._to_internal(v, (self.N, 3)), self._to_internal(C, (self.N, 9)),
+                      self._to_internal(F, (self.N, 9)))
         self.reset()
 
     def set_state(self, x, v=None, C=None, F=None):
@@ -136,8 +147,9 @@ class Simulator:
 
     def reset(self):
         """Restore the scenes' step-0 state (x0, v=0, C=0, F=I), as
-        initialize_ti_field does (simulation_functions.py:301-319)."""
-        self._set_state_internal(self._x0)
+        initialize_ti_field does (simulation_functions.py:301-319), or the
+        state given to :meth:`set_initial_state`."""
+        self._set_state_internal(*self._init)
 
     def get_state(self):
         """Current state in the caller's particle order."""

@@ -103,3 +103,53 @@ def test_adam_identification_reduces_loss():
     h = res['history']
     assert np.all(np.isfinite(h))
     assert h[-1].min() < 0.5 * h[0].min()
+
+
+def test_initial_state_continues_a_rollout():
+    """A rollout restarted from the full state after substep 30 (through
+    set_initial_state) reproduces substeps 30..59 of the continuous rollout:
+    the state carry-over that clip-wise identification relies on."""
+    from diffstir_gb300.scene import Scene
+    from diffstir_gb300.simulator import Simulator
+    T, h = 60, 30
+    sc = S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=2)
+    full = Simulator(sc, max_steps=T)
+    f_full = full.forward(T)[0].cpu().numpy()
+    first = Simulator(sc, max_steps=h)
+    first.forward(h)
+    st = first.get_state()
+    n = sc.n_particles
+    second_sc = Scene(sc.desc, sc.liquid_x, sc.rod_x, sc.container_x, sc.trajectory[h:], sc.params, dict(sc.info))
+    second = Simulator(second_sc, max_steps=T - h)
+    second.set_initial_state(st['x'], st['v'], st['C'].reshape(n, 9), st['F'].reshape(n, 9))
+    f2 = second.forward(T - h)[0].cpu().numpy()
+    ref = f_full[h:]
+    assert np.abs(f2 - ref).max() <= 1e-4 * np.abs(ref).max()
+    # reset() goes back to the carried state, not to x0
+    second.reset()
+    f3 = second.forward(T - h)[0].cpu().numpy()
+    assert np.abs(f3 - ref).max() <= 1e-4 * np.abs(ref).max()
+    for s_ in (full, first, second):
+        s_.close()
+
+
+def test_clip_identification_carries_state():
+    from diffstir_gb300 import identify
+    from diffstir_gb300.simulator import Simulator
+    T, fpc = 60, 30
+    truth = np.array([0.8, 0.0, 0.7, 0.0])
+    sc = S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=0, params=truth)
+    sim = Simulator(sc, max_steps=T)
+    target = sim.forward(T)[0].cpu().numpy()
+    sim.close()
+    sc2 = S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=0, params=(1.0, 0.0, 0.9, 0.0))
+    for carry in ('x', 'full'):
+        res = identify.clip_identify(sc2, target, fpc, carry=carry, restarts=4, iters=8, lr=5e-2, ckpt_every=10,
+                                     free=(0, 2), bounds={0: (0.1, 2.0), 2: (0.4, 1.2)}, seed=1,
+                                     first_clip_factor=2)
+        assert [r['clip'] for r in res] == [0, 1]
+        assert [r['substeps'] for r in res] == [(0, 30), (30, 60)]
+        assert res[0]['history'].shape == (16, 4) and res[1]['history'].shape == (8, 4)
+        for r in res:
+            assert r['status'] == 0 and np.isfinite(r['best_loss'])
+        assert res[0]['best_loss'] < res[0]['history'][0].min()
