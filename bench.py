@@ -353,7 +353,10 @@ def run_ours(args):
         fwd_ms = float(t.item())
 
     # central differences of each scene's loss w.r.t. its free parameters, all
-    # scenes perturbed at once (they are independent), against the adjoint
+    # scenes perturbed at once (they are independent), against the adjoint.
+    # The float atomics of P2G make each rollout's loss vary in its last bits;
+    # `loss_noise_rel` is that variation between two identical rollouts, and
+    # `fd_noise_rel` what it contributes to a difference quotient at each step.
     grad_check = None
     if not args.no_fd:
         _, dp_adj = grad_eval(params)
@@ -367,17 +370,22 @@ def run_ours(args):
             diff = (f - target)[..., 0::2].double()
             return (diff * diff).sum(dim=(1, 2)) / float(B * T * 2)
 
-        errs = {}
-        for i in free:
-            hs = args.fd_h * params[:, i].abs().clamp_min(1e-3)
-            pp, pm = params.clone(), params.clone()
-            pp[:, i] += hs
-            pm[:, i] -= hs
-            fd = (scene_losses(pp) - scene_losses(pm)) / (2.0 * hs.double())
-            ad = dp_adj[:, i].double()
-            errs[names[i]] = float(((ad - fd).abs() / fd.abs().clamp_min(1e-30)).max())
-        grad_check = {'method': 'central differences of each scene loss, h = %g x |param|' % args.fd_h,
-                      'rel_err_max': max(errs.values()), 'rel_err': errs, 'steps': T}
+        l_a, l_b = scene_losses(params), scene_losses(params)
+        noise = (l_a - l_b).abs()
+        grad_check = {'method': 'central differences of each scene loss on the GPU, h = h_rel x |param|',
+                      'steps': T, 'loss_noise_rel': float((noise / l_a.abs().clamp_min(1e-300)).max())}
+        for hr in sorted({args.fd_h, 1e-2}):
+            errs, nse = {}, {}
+            for i in free:
+                hs = hr * params[:, i].abs().clamp_min(1e-3)
+                pp, pm = params.clone(), params.clone()
+                pp[:, i] += hs
+                pm[:, i] -= hs
+                fd = (scene_losses(pp) - scene_losses(pm)) / (2.0 * hs.double())
+                ad = dp_adj[:, i].double()
+                errs[names[i]] = float(((ad - fd).abs() / fd.abs().clamp_min(1e-30)).max())
+                nse[names[i]] = float((noise / (2.0 * hs.double()) / fd.abs().clamp_min(1e-30)).max())
+            grad_check['h_rel=%g' % hr] = {'rel_err': errs, 'rel_err_max': max(errs.values()), 'fd_noise_rel': nse}
 
     # plain comparison: one scene of the workload alone, per-particle scalar
     # atomics, particles in generation order, no graph

@@ -90,3 +90,41 @@ def test_full_size_gravity_only_substep():
     np.testing.assert_allclose(v[:, 2], 0.0, atol=1e-9)
     assert np.all(v[:, 1] <= 0.0) and np.all(v[:, 1] >= g * (1 + 1e-5))
     assert abs(np.median(v[:, 1]) - g) < 1e-4 * abs(g)   # 1e-10 mass floor / ~4e-6 node mass
+
+
+def test_c1_full_length_gradient_vs_fp64_differences():
+    """The 32^3 workload over its full 500 substeps: the GPU adjoint of the
+    force-MSE loss against central differences (h = 1e-3 x |param|) of the
+    FP64 oracle's loss, for K and n; within 1e-3 relative.  The GPU rollout is
+    FP32 throughout, so this bounds rounding drift over the whole horizon as
+    well as the adjoint itself."""
+    T = 500
+    sc = rounded(S.synthetic_scene('C1', seed=0, n_steps=T))
+    truth = np.array([0.5, 0.0, 0.7, 0.0])
+    f_t, _, st = oracle.rollout(sc.desc, truth, sc.trajectory, T, sc.x0(), precision='f64', threads=THREADS)
+    assert st == 0
+    p = np.array([0.8, 0.0, 0.9, 0.0])
+
+    def oracle_loss(pp):
+        f, _, s_ = oracle.rollout(sc.desc, pp, sc.trajectory, T, sc.x0(), precision='f64', threads=THREADS)
+        assert s_ == 0
+        d = (f - f_t)[:, 0::2]
+        return (d * d).sum() / d.size
+
+    sim = Simulator(sc, max_steps=T)
+    sim.set_params(torch.tensor(p[None], dtype=torch.float32, device='cuda'))
+    sim.reset()
+    f = sim.forward(T, ckpt_every=50, record=True)[0].double().cpu().numpy()
+    d = (f - f_t)[:, 0::2]
+    w = np.zeros((1, T, 3))
+    w[0, :, 0::2] = 2.0 * d / d.size
+    dp = sim.backward(torch.as_tensor(w, dtype=torch.float32, device='cuda'))[0].cpu().numpy()
+    assert sim.status() == 0
+    sim.close()
+    for i in (0, 2):
+        h = 1e-3 * abs(p[i])
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (oracle_loss(pp) - oracle_loss(pm)) / (2 * h)
+        assert abs(dp[i] - fd) <= 1e-3 * abs(fd), (i, dp[i], fd)
