@@ -157,6 +157,25 @@ struct DstirHandle {
     BrickInfo* bricks = nullptr;
     int n_bricks = 0;
 
+    // periodic re-sort of the particle order (per-particle variants): every K
+    // substeps of a rollout, at the checkpoint boundaries of a recorded one
+    int resort = 1;             // option "resort": 0 never
+    int max_n = 0;              // largest n_grid of the batch
+    int* rs_cnt = nullptr;      // [G+1]
+    int* rs_start = nullptr;    // [G+2]
+    int* rs_bsum = nullptr;
+    int* rs_key = nullptr;      // [stride]
+    int* rs_rank = nullptr;     // [stride]
+    int* rs_sorted = nullptr;   // [stride]
+    int* rs_dest = nullptr;     // [rs_dest_slots][stride]: permutation that made checkpoint slot c
+    long long rs_dest_slots = 0;
+    int* perm_cur = nullptr;    // [stride] caller index of each internal position
+    int* perm_tmp = nullptr;    // [stride]
+    int* perm_rec0 = nullptr;   // [stride] perm_cur at the start of the recorded rollout
+    bool perm_id = true;        // perm_cur is the identity
+    bool rec_perm_id = true;
+    bool rec_resort = false;
+
     Profiler prof;
     long long launches = 0;  // kernel launches issued since the counter was reset
 
@@ -484,6 +503,7 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
         if (d.j_mode == DSTIR_J_SVD) h->any_svd = true;
         p0 += (long long)d.n_liquid + d.n_rod + d.n_container;
         g0 += (long long)d.n_grid * d.n_grid * d.n_grid;
+        h->max_n = std::max(h->max_n, (int)d.n_grid);
     }
     h->N = p0;
     h->stride = std::max<long long>((p0 + 31) / 32 * 32, 32);
@@ -508,6 +528,9 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
         (rc = dalloc(h, &h->pgrad, (size_t)max_steps * batch * 4, "parameter gradients")) ||
         (rc = dalloc(h, &h->counters, (size_t)3 * batch, "counters")) ||
         (rc = dalloc(h, &h->status, 1, "status")) || (rc = dalloc(h, &h->bricks, h->bricks_h.size(), "bricks")) ||
+        (rc = dalloc(h, &h->perm_cur, (size_t)h->stride, "particle order")) ||
+        (rc = dalloc(h, &h->perm_tmp, (size_t)h->stride, "particle order")) ||
+        (rc = dalloc(h, &h->perm_rec0, (size_t)h->stride, "particle order")) ||
         (rc = ensure_grid_slots(h, 1)) || (rc = build_tables(h))) {
         std::string msg = h->err;
         dstir_destroy(h);
@@ -523,6 +546,10 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
     if (e == cudaSuccess) e = cudaMemset(h->params, 0, (size_t)batch * 4 * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(h->traj, 0, (size_t)batch * (max_steps + 1) * 3 * sizeof(float));
     if (e == cudaSuccess) e = cudaMemset(h->work, 0, 3 * slot_floats(h) * sizeof(float));
+    if (e == cudaSuccess) {
+        launch_iota(h->perm_cur, h->stride, 0);
+        e = cudaDeviceSynchronize();
+    }
     if (e != cudaSuccess) {
         dstir_destroy(h);
         return DSTIR_ECUDA;
@@ -546,7 +573,8 @@ void dstir_destroy(DstirHandle* h) {
     void* ptrs[] = {h->sc, h->blk, h->gblk, h->work, h->ckpt, h->seg, h->pm, h->vo, h->ga, h->pmb, h->adj,
                     h->traj, h->params, h->models, h->force_scratch, h->pgrad, h->partial, h->counters, h->status,
                     h->cnt, h->bkey, h->brank, h->bsum, h->cell_start, h->perm, h->fbuf, h->dfbuf, h->dpbuf,
-                    h->bricks};
+                    h->bricks, h->rs_cnt, h->rs_start, h->rs_bsum, h->rs_key, h->rs_rank, h->rs_sorted,
+                    h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -567,13 +595,16 @@ int dstir_set_state(DstirHandle* h, const float* x, const float* v, const float*
     h->cur = 0;
     h->recorded = false;
     timed(h, K_OTHER, S(stream), [&] { launch_pack_state(x, v, C, F, h->work, h->stride, h->N, S(stream)); });
+    if (!h->perm_id) launch_iota(h->perm_cur, h->stride, S(stream));
+    h->perm_id = true;
     CUDA_TRY(h, cudaGetLastError());
     return DSTIR_OK;
 }
 
 int dstir_get_state(DstirHandle* h, float* x, float* v, float* C, float* F, void* stream) {
     if (!h) return DSTIR_EINVAL;
-    launch_unpack_state(h->work + (size_t)h->cur * slot_floats(h), h->stride, h->N, x, v, C, F, S(stream));
+    launch_unpack_state(h->work + (size_t)h->cur * slot_floats(h), h->stride, h->N, x, v, C, F,
+                        h->perm_id ? nullptr : h->perm_cur, S(stream));
     CUDA_TRY(h, cudaGetLastError());
     return DSTIR_OK;
 }
@@ -650,25 +681,113 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
     }
 }
 
+bool resort_on(const DstirHandle* h) { return h->resort && !binned(h) && h->max_n <= 1024; }
+
+int ensure_resort(DstirHandle* h, long long dest_slots) {
+    int rc;
+    if (!h->rs_cnt) {
+        if ((rc = dalloc(h, &h->rs_cnt, (size_t)h->G + 1, "re-sort counts"))) return rc;
+        CUDA_TRY(h, cudaMemset(h->rs_cnt, 0, ((size_t)h->G + 1) * sizeof(int)));
+        if ((rc = dalloc(h, &h->rs_start, (size_t)h->G + 2, "re-sort cell starts")) ||
+            (rc = dalloc(h, &h->rs_bsum, (size_t)bin_scan_blocks(h->G), "re-sort scan")) ||
+            (rc = dalloc(h, &h->rs_key, (size_t)h->stride, "re-sort keys")) ||
+            (rc = dalloc(h, &h->rs_rank, (size_t)h->stride, "re-sort ranks")) ||
+            (rc = dalloc(h, &h->rs_sorted, (size_t)h->stride, "re-sort list")))
+            return rc;
+    }
+    if (dest_slots > h->rs_dest_slots) {
+        if ((rc = dalloc(h, &h->rs_dest, (size_t)(dest_slots * h->stride), "re-sort permutations"))) return rc;
+        h->rs_dest_slots = dest_slots;
+    }
+    return DSTIR_OK;
+}
+
+// Re-sort state `in` into `out` (different slots); dest receives the
+// permutation; perm_cur follows the particles.
+void enqueue_resort(DstirHandle* h, const float* in, float* out, int* dest, cudaStream_t st) {
+    ResortArgs r;
+    r.sc = h->sc;
+    r.blk = h->blk;
+    r.in = in;
+    r.out = out;
+    r.stride = h->stride;
+    r.cnt = h->rs_cnt;
+    r.cell_start = h->rs_start;
+    r.bsum = h->rs_bsum;
+    r.G = h->G;
+    r.key = h->rs_key;
+    r.rank = h->rs_rank;
+    r.sorted = h->rs_sorted;
+    r.dest = dest;
+    r.perm_in = h->perm_cur;
+    r.perm_out = h->perm_tmp;
+    h->launches += 6;  // seven kernels; timed() counts one
+    timed(h, K_OTHER, st, [&] { launch_resort(r, h->n_blocks, h->block, h->max_n, h->B, st); });
+    cudaMemcpyAsync(h->perm_cur, h->perm_tmp, (size_t)h->N * sizeof(int), cudaMemcpyDeviceToDevice, st);
+}
+
+// Number of re-sorts in a rollout of nsteps substeps, chunk length K.
+long long resort_count(const DstirHandle* h, int nsteps, int K) {
+    return resort_on(h) && K > 0 && nsteps > K ? (nsteps - 1) / K : 0;
+}
+
+// Work slot that holds the final state of a forward rollout (the same
+// arithmetic as enqueue_forward, for replayed graphs).
+int forward_final_slot(const DstirHandle* h, int nsteps, int K, bool record) {
+    int a = h->cur;
+    if (!resort_count(h, nsteps, K)) return (a + nsteps) % 3;
+    for (int k0 = 0;;) {
+        int L = std::min(K, nsteps - k0);
+        int out = (a + L) % 3;
+        if (k0 + L >= nsteps) return out;
+        a = record ? out : (out + 1) % 3;
+        k0 += L;
+    }
+}
+
 // Enqueue a forward rollout; forces go to h->fbuf [B][max_steps][3] at fo = k.
-// State k lives in checkpoint slot k/K when recording and k is a multiple of
-// K, else in work slot (cur + k) % 3; returns the work slot of the final state.
+// The rollout runs in chunks of K substeps.  Chunk c starts from checkpoint
+// slot c when recording, else from a work slot; its intermediate states
+// rotate over the three work slots.  With the re-sort on, the state at the
+// end of every chunk but the last is re-sorted into the next chunk's start
+// slot; otherwise the chunks simply continue ((cur + k) % 3).  Returns the
+// work slot of the final state.
 int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, cudaStream_t st) {
     size_t sf = slot_floats(h);
     float* W[3] = {h->work, h->work + sf, h->work + 2 * sf};
     const int cur = h->cur;
-    auto slot = [&](int k) -> float* {
-        if (record && k % K == 0 && k < nsteps) return h->ckpt + (size_t)(k / K) * sf;
-        return W[(cur + k) % 3];
-    };
-    if (record) cudaMemcpyAsync(h->ckpt, W[cur], sf * sizeof(float), cudaMemcpyDeviceToDevice, st);
+    if (record) {
+        cudaMemcpyAsync(h->ckpt, W[cur], sf * sizeof(float), cudaMemcpyDeviceToDevice, st);
+        cudaMemcpyAsync(h->perm_rec0, h->perm_cur, (size_t)h->N * sizeof(int), cudaMemcpyDeviceToDevice, st);
+    }
     cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st);
     auto grids = [&](int, float4*& pm, float4*& vo) {
         pm = h->pm;
         vo = h->vo;
     };
-    chain_forward(h, t0, nsteps, slot, grids, h->fbuf, (long long)h->max_steps * 3, 0, 1, false, false, st);
-    return (cur + nsteps) % 3;
+    if (!resort_count(h, nsteps, K)) {
+        auto slot = [&](int k) -> float* {
+            if (record && k % K == 0 && k < nsteps) return h->ckpt + (size_t)(k / K) * sf;
+            return W[(cur + k) % 3];
+        };
+        chain_forward(h, t0, nsteps, slot, grids, h->fbuf, (long long)h->max_steps * 3, 0, 1, false, false, st);
+        return (cur + nsteps) % 3;
+    }
+    int a = cur;
+    float* in = record ? h->ckpt : W[cur];
+    for (int c = 0, k0 = 0;; ++c) {
+        const int L = std::min(K, nsteps - k0);
+        auto slot = [&](int j) -> float* { return j == 0 ? in : W[(a + j) % 3]; };
+        chain_forward(h, t0 + k0, L, slot, grids, h->fbuf, (long long)h->max_steps * 3, k0, 1, false, false, st);
+        const int out = (a + L) % 3;
+        if (k0 + L >= nsteps) return out;
+        float* next = record ? h->ckpt + (size_t)(c + 1) * sf : W[(out + 1) % 3];
+        int* dest = h->rs_dest + (size_t)(record ? c + 1 : 0) * h->stride;
+        enqueue_resort(h, W[out], next, dest, st);
+        in = next;
+        a = record ? out : (out + 1) % 3;
+        k0 += L;
+    }
 }
 
 // Run `body(stream)` either directly on `st` or as a cached CUDA graph
@@ -727,7 +846,8 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
     cudaStream_t st = S(stream);
     h->recorded = false;
     if (nsteps == 0) return DSTIR_OK;
-    int K = record ? std::min(ckpt_every, nsteps) : 1;
+    // K: checkpoint interval of a recorded rollout, and the re-sort interval
+    int K = ckpt_every > 0 ? std::min(ckpt_every, nsteps) : nsteps;
     long long nseg = record ? (nsteps + K - 1) / K : 0;
     int rc;
     if (record && nseg > h->ckpt_slots) {
@@ -735,14 +855,16 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
         h->ckpt_slots = nseg;
     }
     if (binned(h) && (rc = ensure_bin_slots(h, 1))) return rc;
-    long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch, h->p2g_variant * 16 + h->fuse,
-                         h->block * 4096 + h->gblock};
-    int final_slot = 0;
+    const long long nres = resort_count(h, nsteps, K);
+    if (nres && (rc = ensure_resort(h, record ? nseg : 1))) return rc;
+    long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch,
+                         h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0), h->block * 4096 + h->gblock};
     rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want,
-                         [&](cudaStream_t s2) { final_slot = enqueue_forward(h, t0, nsteps, K, record != 0, s2); });
+                         [&](cudaStream_t s2) { enqueue_forward(h, t0, nsteps, K, record != 0, s2); });
     if (rc) return rc;
-    final_slot = (h->cur + nsteps) % 3;  // also when the chain ran as a replayed graph
-    h->cur = final_slot;
+    const bool start_perm_id = h->perm_id;
+    h->cur = forward_final_slot(h, nsteps, K, record != 0);  // also when the chain ran as a replayed graph
+    if (nres) h->perm_id = false;
     if (force_out)
         CUDA_TRY(h, cudaMemcpy2DAsync(force_out, (size_t)nsteps * 3 * sizeof(float), h->fbuf,
                                       (size_t)h->max_steps * 3 * sizeof(float), (size_t)nsteps * 3 * sizeof(float),
@@ -752,6 +874,8 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
         h->rec_t0 = t0;
         h->rec_n = nsteps;
         h->rec_K = K;
+        h->rec_resort = nres > 0;
+        h->rec_perm_id = start_perm_id;
     }
     return DSTIR_OK;
 }
@@ -861,6 +985,15 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
                 }
             }
         }
+        if (h->rec_resort && sgi > 0) {
+            // checkpoint sgi was re-sorted from the state that ended segment
+            // sgi-1: bring the adjoint of state s0 back to that order
+            float* adj0 = A[(n - s0) & 1];
+            timed(h, K_OTHER, st, [&] {
+                launch_unpermute(adj0, h->seg, h->rs_dest + (size_t)sgi * h->stride, h->stride, h->N, st);
+            });
+            cudaMemcpyAsync(adj0, h->seg, sf * sizeof(float), cudaMemcpyDeviceToDevice, st);
+        }
     }
     cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st);
     timed(h, K_OTHER, st, [&] { launch_reduce_pgrad(h->pgrad, n, h->B, h->dpbuf, st); });
@@ -891,7 +1024,7 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
                                   (size_t)n * 3 * sizeof(float), (size_t)n * 3 * sizeof(float), (size_t)h->B,
                                   cudaMemcpyDeviceToDevice, st));
     long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant * 16 + h->fuse * 2 + h->fuse_adj,
-                         h->block * 4096 + h->gblock, 0, 0};
+                         h->block * 4096 + h->gblock, h->rec_resort ? 1 : 0, 0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, [&](cudaStream_t s2) { enqueue_backward(h, s2); });
     if (rc) return rc;
@@ -901,7 +1034,10 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
                                     st));
     if (dL_dx0 || dL_dv0 || dL_dC0 || dL_dF0)
         timed(h, K_OTHER, st,
-              [&] { launch_unpack_state(A[final_nx], h->stride, h->N, dL_dx0, dL_dv0, dL_dC0, dL_dF0, st); });
+              [&] {
+                  launch_unpack_state(A[final_nx], h->stride, h->N, dL_dx0, dL_dv0, dL_dC0, dL_dF0,
+                                      h->rec_perm_id ? nullptr : h->perm_rec0, st);
+              });
     CUDA_TRY(h, cudaGetLastError());
     return DSTIR_OK;
 }
@@ -936,6 +1072,11 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     }
     if (!strcmp(key, "graph")) {
         h->use_graph = value ? 1 : 0;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "resort")) {
+        h->resort = value ? 1 : 0;
+        h->recorded = false;
         return DSTIR_OK;
     }
     if (!strcmp(key, "fuse_adj")) {
@@ -985,6 +1126,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "brick_scatter")) *value = h->brick_scatter;
     else if (!strcmp(key, "fuse")) *value = h->fuse;
     else if (!strcmp(key, "fuse_adj")) *value = h->fuse_adj;
+    else if (!strcmp(key, "resort")) *value = h->resort;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

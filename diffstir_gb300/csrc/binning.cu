@@ -197,6 +197,13 @@ void launch_bin(const BinArgs& b, int n_blocks, int block, cudaStream_t st) {
 
 int bin_scan_blocks(long long G) { return (int)((G + 1 + SCAN_CHUNK - 1) / SCAN_CHUNK); }
 
+void launch_scan(int* cnt, long long n, int* bsum, int* cell_start, cudaStream_t st) {
+    int nb = (int)((n + SCAN_CHUNK - 1) / SCAN_CHUNK);
+    scan_reduce_kernel<<<nb, SCAN_THREADS, 0, st>>>(cnt, n, bsum);
+    scan_top_kernel<<<1, 1024, 0, st>>>(bsum, nb);
+    scan_apply_kernel<<<nb, SCAN_THREADS, 0, st>>>(cnt, n, bsum, cell_start);
+}
+
 // ---------------------------------------------------------------------------
 // binned P2G: one thread per cell
 // ---------------------------------------------------------------------------

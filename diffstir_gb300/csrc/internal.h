@@ -120,8 +120,41 @@ void launch_p2g_adj_brick(const AdjArgs& a, const BrickInfo* bricks, int n_brick
 
 void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
                        long long stride, long long n, cudaStream_t s);
+// perm (optional): internal position p goes to caller index perm[p]
 void launch_unpack_state(const float* st, long long stride, long long n, float* x, float* v, float* C,
-                         float* F, cudaStream_t s);
+                         float* F, const int* perm, cudaStream_t s);
+void launch_iota(int* a, long long n, cudaStream_t s);
+
+// exclusive scan of cnt[0, n) into cell_start[0, n] (cell_start[n] = total);
+// zeroes cnt.  bsum: bin_scan_blocks(n - 1) entries.
+void launch_scan(int* cnt, long long n, int* bsum, int* cell_start, cudaStream_t st);
+
+// Re-sort of the liquid particles of every scene into the interleaved order
+// (stencil-base row (i, j), then rank inside the base cell, then k), so that
+// the lanes of a warp hold particles of consecutive base cells of one grid row
+// again.  Rod and container particles keep their positions.
+struct ResortArgs {
+    const SceneDev* sc;
+    const BlockInfo* blk;
+    const float* in;         // state in the current order
+    float* out;              // state in the new order
+    long long stride;
+    int* cnt;                // [G+1], zero on entry and on exit
+    int* cell_start;         // [G+2]
+    int* bsum;               // bin_scan_blocks(G) entries
+    long long G;             // grid nodes of all scenes
+    int* key;                // [N] base cell of each liquid particle
+    int* rank;               // [N] rank inside the base cell
+    int* sorted;             // [N] liquid particles in base-cell order
+    int* dest;               // [N] new position of each particle (identity for rod/container)
+    const int* perm_in;      // [N] caller index of each current position
+    int* perm_out;           // [N] caller index of each new position
+};
+void launch_resort(const ResortArgs& r, int n_blocks, int block, int max_n, int n_scenes, cudaStream_t st);
+// out[c][p] = in[c][dest[p]]: the adjoint of the re-sort (adjoint in the new
+// order -> adjoint in the order before)
+void launch_unpermute(const float* in, float* out, const int* dest, long long stride, long long n,
+                      cudaStream_t st);
 void launch_reduce_pgrad(const float* pgrad, int T, int B, float* out, cudaStream_t s);
 
 void launch_svd3(const float* A, float* U, float* S, float* V, long long n, cudaStream_t s);

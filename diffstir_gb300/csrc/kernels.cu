@@ -833,19 +833,25 @@ __global__ void pack_state_kernel(const float* x, const float* v, const float* C
 }
 
 __global__ void unpack_state_kernel(const float* st, long long stride, long long n, float* x, float* v, float* C,
-                                    float* F) {
+                                    float* F, const int* perm) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
     if (p >= n) return;
+    long long q = perm ? (long long)perm[p] : p;
 #pragma unroll
     for (int c = 0; c < 3; ++c) {
-        if (x) x[p * 3 + c] = st[(OX + c) * stride + p];
-        if (v) v[p * 3 + c] = st[(OV + c) * stride + p];
+        if (x) x[q * 3 + c] = st[(OX + c) * stride + p];
+        if (v) v[q * 3 + c] = st[(OV + c) * stride + p];
     }
 #pragma unroll
     for (int c = 0; c < 9; ++c) {
-        if (C) C[p * 9 + c] = st[(OC + c) * stride + p];
-        if (F) F[p * 9 + c] = st[(OF + c) * stride + p];
+        if (C) C[q * 9 + c] = st[(OC + c) * stride + p];
+        if (F) F[q * 9 + c] = st[(OF + c) * stride + p];
     }
+}
+
+__global__ void iota_kernel(int* a, long long n) {
+    long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (p < n) a[p] = (int)p;
 }
 
 // out[b*4+c] = sum_t pgrad[(t*B+b)*4+c], one block per (b, c), fixed order
@@ -926,9 +932,12 @@ void launch_pack_state(const float* x, const float* v, const float* C, const flo
                        long long stride, long long n, cudaStream_t s) {
     if (n > 0) pack_state_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(x, v, C, F, st, stride, n);
 }
+void launch_iota(int* a, long long n, cudaStream_t s) {
+    if (n > 0) iota_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(a, n);
+}
 void launch_unpack_state(const float* st, long long stride, long long n, float* x, float* v, float* C,
-                         float* F, cudaStream_t s) {
-    if (n > 0) unpack_state_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st, stride, n, x, v, C, F);
+                         float* F, const int* perm, cudaStream_t s) {
+    if (n > 0) unpack_state_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(st, stride, n, x, v, C, F, perm);
 }
 void launch_reduce_pgrad(const float* pgrad, int T, int B, float* out, cudaStream_t s) {
     if (B > 0) reduce_pgrad_kernel<<<B * 4, 256, 0, s>>>(pgrad, T, B, out);

@@ -67,9 +67,10 @@ def fixture_scene(name, model):
 VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse': 1, 'fuse_adj': 0},
             {'p2g': 0, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 2}, {'p2g': 3},
             {'p2g': 3, 'brick_scatter': 0}, {'p2g': 3, 'brick_scatter': 2}, {'p2g': 3, 'brick_gather': 0},
-            {'p2g': 3, 'graph': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}]
+            {'p2g': 3, 'graph': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 4, 'resort': 0},
+            {'p2g': 4, 'graph': 1}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
-               'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused']
+               'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
@@ -124,6 +125,54 @@ def test_forward_states_match_oracle():
     assert rel(st['v'].cpu().numpy(), last[:, 3:6]) < 1e-3
     assert rel(st['C'].cpu().numpy().reshape(-1, 9), last[:, 6:15]) < 1e-3
     assert rel(st['F'].cpu().numpy().reshape(-1, 9), last[:, 15:24]) < 1e-4
+
+
+def test_forward_states_match_oracle_after_resorts():
+    """A rollout re-sorted every 7 substeps returns its state in the caller's
+    particle order."""
+    T = 30
+    sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=4, n_steps=T, seed=2))
+    sim = Simulator(sc, max_steps=T, options={'p2g': 4})
+    sim.forward(T, ckpt_every=7)
+    st = sim.get_state()
+    _, states, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, sc.x0(), return_states=True)
+    last = states[T]
+    assert rel(st['x'].cpu().numpy(), last[:, 0:3]) < 1e-5
+    assert rel(st['v'].cpu().numpy(), last[:, 3:6]) < 1e-3
+    assert rel(st['F'].cpu().numpy().reshape(-1, 9), last[:, 15:24]) < 1e-4
+
+
+@pytest.mark.parametrize('opts', [{'p2g': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1},
+                                  {'p2g': 4, 'graph': 1}], ids=['vec', 'warp', 'warp-fused', 'warp-graph'])
+def test_resort_matches_fixed_order(opts):
+    """Re-sorting the particles at every checkpoint changes only the order of
+    the float atomics: forces, final state, parameter gradient and the
+    adjoint of the step-0 state (in the caller's order) match the run without
+    re-sort.  Two scenes of different sizes, ten segments, twice in a row."""
+    T, K = 40, 4
+    scenes = [rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=6)),
+              rounded(S.small_synthetic_scene(n_grid=20, ppc=3, n_steps=T, seed=7))]
+    wts = torch.as_tensor(np.random.default_rng(4).normal(size=(2, T, 3)), dtype=torch.float32, device='cuda')
+    out = {}
+    for rs in (0, 1):
+        sim = Simulator(scenes, max_steps=T, options=dict(opts, resort=rs))
+        for rep in range(2):
+            sim.reset()
+            f = sim.forward(T, ckpt_every=K, record=True).cpu().numpy()
+            st = {k: v.cpu().numpy() for k, v in sim.get_state().items()}
+            dp, ds = sim.backward(wts, want_state0=True)
+            out[(rs, rep)] = (f, st, dp.cpu().numpy(), {k: v.cpu().numpy() for k, v in ds.items()})
+        assert sim.status() == 0
+        sim.close()
+    f0, st0, dp0, ds0 = out[(0, 0)]
+    for key in ((0, 1), (1, 0), (1, 1)):
+        f, st, dp, ds = out[key]
+        assert rel(f, f0) < 1e-5
+        for k in 'xvCF':
+            assert rel(st[k], st0[k]) < 1e-4, k
+        assert rel(dp, dp0) < 1e-4
+        for k in 'xvCF':
+            assert rel(ds[k], ds0[k]) < 1e-3, k
 
 
 def test_checkpoint_interval_invariance():
