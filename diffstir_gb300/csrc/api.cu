@@ -160,6 +160,7 @@ struct DstirHandle {
     // periodic re-sort of the particle order (per-particle variants): every K
     // substeps of a rollout, at the checkpoint boundaries of a recorded one
     int resort = 1;             // option "resort": 0 never
+    int tight = 0;              // option "tight": register caps for G2P and the adjoint kernels
     int max_n = 0;              // largest n_grid of the batch
     int* rs_cnt = nullptr;      // [G+1]
     int* rs_start = nullptr;    // [G+2]
@@ -401,7 +402,7 @@ void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot
                              h->nbins_brick, st);
         });
     else
-        timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st); });
+        timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st, h->tight); });
 }
 
 void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st, int bin_slot = 0) {
@@ -417,7 +418,7 @@ void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st, int bin_
         });
     } else {
         const int var = h->p2g_variant;  // P2G_PLAIN, P2G_VEC or P2G_WARP here
-        timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st); });
+        timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st, h->tight); });
     }
     timed(h, K_GRID_ADJ, st, [&] { launch_grid_adj(a, h->n_gblocks, h->gblock, st); });
     if (h->p2g_variant == P2G_BRICK && h->brick_gather)
@@ -426,7 +427,7 @@ void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st, int bin_
                                  h->nbins_brick, h->any_svd, st);
         });
     else
-        timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st); });
+        timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st, h->tight); });
 }
 
 }  // namespace
@@ -676,7 +677,7 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
             timed(h, K_G2P_P2G, st,
                   [&] { launch_g2p_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st); });
         } else if (!skip_last_g2p) {
-            timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st); });
+            timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st, h->tight); });
         }
     }
 }
@@ -969,7 +970,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             const int var = h->p2g_variant;  // P2G_PLAIN, P2G_VEC or P2G_WARP here
             {
                 AdjArgs a = adj_args(L - 1);
-                timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st); });
+                timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st, h->tight); });
             }
             for (int k = L - 1; k >= 0; --k) {
                 AdjArgs a = adj_args(k);
@@ -981,7 +982,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
                     timed(h, K_P2G_ADJ_G2P_ADJ, st,
                           [&] { launch_p2g_adj_g2p_adj(a, h->n_blocks, h->block, var, h->any_svd, st); });
                 } else {
-                    timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st); });
+                    timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st, h->tight); });
                 }
             }
         }
@@ -1079,6 +1080,11 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         h->recorded = false;
         return DSTIR_OK;
     }
+    if (!strcmp(key, "tight")) {
+        h->tight = value ? 1 : 0;
+        ++h->epoch;
+        return DSTIR_OK;
+    }
     if (!strcmp(key, "fuse_adj")) {
         h->fuse_adj = value ? 1 : 0;
         h->recorded = false;
@@ -1127,6 +1133,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "fuse")) *value = h->fuse;
     else if (!strcmp(key, "fuse_adj")) *value = h->fuse_adj;
     else if (!strcmp(key, "resort")) *value = h->resort;
+    else if (!strcmp(key, "tight")) *value = h->tight;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

@@ -176,7 +176,11 @@ __global__ void __launch_bounds__(256) grid_kernel(FwdArgs a) {
     }
 }
 
-__global__ void __launch_bounds__(256) g2p_kernel(FwdArgs a) {
+// MINB: minimum resident blocks per SM the register allocation must allow
+// (1: unconstrained; the "tight" option selects 4 for G2P and 3 for the
+// adjoint kernels, trading a few spilled registers for occupancy)
+template <int MINB>
+__global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
@@ -433,8 +437,8 @@ __global__ void __launch_bounds__(256) g2p_p2g_kernel(FwdArgs a) {
 // ---------------------------------------------------------------------------
 // adjoint
 // ---------------------------------------------------------------------------
-template <int VARIANT>
-__global__ void __launch_bounds__(256) g2p_adj_kernel(AdjArgs a) {
+template <int VARIANT, int MINB>
+__global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float fb[3];
@@ -609,8 +613,8 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(AdjArgs a) {
 }
 
 // P2G adjoint, one thread per particle (pieces in adjoint.cuh).
-template <bool SVDJ>
-__global__ void __launch_bounds__(256) p2g_adj_kernel(AdjArgs a) {
+template <bool SVDJ, int MINB>
+__global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
@@ -882,8 +886,12 @@ void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svd
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks > 0) grid_kernel<<<n_gblocks, gblock, 0, st>>>(a);
 }
-void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st) {
-    if (n_blocks > 0) g2p_kernel<<<n_blocks, block, 0, st>>>(a);
+void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, bool tight) {
+    if (n_blocks <= 0) return;
+    if (tight)
+        g2p_kernel<4><<<n_blocks, block, 0, st>>>(a);
+    else
+        g2p_kernel<1><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st) {
     if (n_blocks <= 0) return;
@@ -897,24 +905,28 @@ void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool
         svdj ? g2p_p2g_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
              : g2p_p2g_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
 }
-void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st) {
+void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st, bool tight) {
     if (n_blocks <= 0) return;
     if (variant == P2G_PLAIN)
-        g2p_adj_kernel<P2G_PLAIN><<<n_blocks, block, 0, st>>>(a);
+        g2p_adj_kernel<P2G_PLAIN, 1><<<n_blocks, block, 0, st>>>(a);
     else if (variant == P2G_WARP)
-        g2p_adj_kernel<P2G_WARP><<<n_blocks, block, 0, st>>>(a);
+        tight ? g2p_adj_kernel<P2G_WARP, 3><<<n_blocks, block, 0, st>>>(a)
+              : g2p_adj_kernel<P2G_WARP, 1><<<n_blocks, block, 0, st>>>(a);
     else
-        g2p_adj_kernel<P2G_VEC><<<n_blocks, block, 0, st>>>(a);
+        tight ? g2p_adj_kernel<P2G_VEC, 3><<<n_blocks, block, 0, st>>>(a)
+              : g2p_adj_kernel<P2G_VEC, 1><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks > 0) grid_adj_kernel<<<n_gblocks, gblock, 0, st>>>(a);
 }
-void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st) {
+void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st, bool tight) {
     if (n_blocks <= 0) return;
     if (svdj)
-        p2g_adj_kernel<true><<<n_blocks, block, 0, st>>>(a);
+        p2g_adj_kernel<true, 1><<<n_blocks, block, 0, st>>>(a);
+    else if (tight)
+        p2g_adj_kernel<false, 3><<<n_blocks, block, 0, st>>>(a);
     else
-        p2g_adj_kernel<false><<<n_blocks, block, 0, st>>>(a);
+        p2g_adj_kernel<false, 1><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st) {
     if (n_blocks <= 0) return;
