@@ -152,7 +152,7 @@ def test_resort_matches_fixed_order(opts):
     re-sort.  Two scenes of different sizes, ten segments, twice in a row."""
     T, K = 40, 4
     scenes = [rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=6)),
-              rounded(S.small_synthetic_scene(n_grid=20, ppc=3, n_steps=T, seed=7))]
+              rounded(S.small_synthetic_scene(n_grid=20, ppc=4, n_steps=T, seed=7))]
     wts = torch.as_tensor(np.random.default_rng(4).normal(size=(2, T, 3)), dtype=torch.float32, device='cuda')
     out = {}
     for rs in (0, 1):
