@@ -76,7 +76,7 @@ def parse():
     ap.add_argument('--fuse', type=int, default=None, help='1: G2P(f) fused with P2G(f+1)')
     ap.add_argument('--fuse-adj', type=int, default=None, help='1: P2G adjoint of f fused with G2P adjoint of f-1')
     ap.add_argument('--resort', type=int, default=None, help='1: re-sort the particle order at every checkpoint')
-    ap.add_argument('--tight', type=int, default=None, help='1: register caps for G2P and the adjoint kernels')
+    ap.add_argument('--tight', type=int, default=None, help='register-cap level of the particle kernels: 0, 1 or 2')
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')

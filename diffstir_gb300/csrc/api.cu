@@ -160,7 +160,7 @@ struct DstirHandle {
     // periodic re-sort of the particle order (per-particle variants): every K
     // substeps of a rollout, at the checkpoint boundaries of a recorded one
     int resort = 1;             // option "resort": 0 never
-    int tight = 0;              // option "tight": register caps for G2P and the adjoint kernels
+    int tight = 1;              // option "tight": register-cap level of the particle kernels (0, 1, 2)
     int max_n = 0;              // largest n_grid of the batch
     int* rs_cnt = nullptr;      // [G+1]
     int* rs_start = nullptr;    // [G+2]
@@ -393,7 +393,7 @@ void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot
                 launch_p2g_cell(a, b.cell_start, b.perm, h->n_gblocks, h->gblock, h->G, h->any_svd, st);
             });
     } else {
-        timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st); });
+        timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st, h->tight); });
     }
     timed(h, K_GRID, st, [&] { launch_grid(a, h->n_gblocks, h->gblock, st); });
     if (h->p2g_variant == P2G_BRICK && h->brick_gather)
@@ -662,7 +662,7 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
         float4 *pm, *vo;
         grids(0, pm, vo);
         FwdArgs a = fwd_args(h, slot(0), slot(1), pm, vo, t0, force, fstride, fo0, clear_pm);
-        timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st); });
+        timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st, h->tight); });
     }
     for (int k = 0; k < nsteps; ++k) {
         float4 *pm, *vo;
@@ -675,7 +675,7 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
             a.next2 = slot(k + 2);
             a.pm_next = pmn;
             timed(h, K_G2P_P2G, st,
-                  [&] { launch_g2p_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st); });
+                  [&] { launch_g2p_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st, h->tight); });
         } else if (!skip_last_g2p) {
             timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st, h->tight); });
         }
@@ -980,7 +980,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
                     a.vo2 = h->vo + (size_t)(k - 1) * h->G;
                     a.adj_prev = A[(n - (s0 + k - 1)) & 1];
                     timed(h, K_P2G_ADJ_G2P_ADJ, st,
-                          [&] { launch_p2g_adj_g2p_adj(a, h->n_blocks, h->block, var, h->any_svd, st); });
+                          [&] { launch_p2g_adj_g2p_adj(a, h->n_blocks, h->block, var, h->any_svd, st, h->tight); });
                 } else {
                     timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st, h->tight); });
                 }
@@ -1081,7 +1081,8 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         return DSTIR_OK;
     }
     if (!strcmp(key, "tight")) {
-        h->tight = value ? 1 : 0;
+        if (value < 0 || value > 2) return fail(h, DSTIR_EINVAL, "tight %lld not in 0..2", (long long)value);
+        h->tight = (int)value;
         ++h->epoch;
         return DSTIR_OK;
     }

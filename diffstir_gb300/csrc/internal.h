@@ -87,18 +87,21 @@ struct BinArgs {
 // vector atomics after warp run aggregation of the k-consecutive stencil rows
 enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_CELL = 2, P2G_BRICK = 3, P2G_WARP = 4 };
 
-void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st);
+// tight: register-cap level of the particle kernels (0, 1 or 2; see kernels.cu)
+void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st, int tight = 0);
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st);
-void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, bool tight = false);
+void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight = 0);
 // G2P of substep f (into a.next) fused with the stress and P2G scatter of
 // substep f+1 (F into a.next2, grid into a.pm_next)
-void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st);
+void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st,
+                    int tight = 0);
 
-void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st, bool tight = false);
+void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st, int tight = 0);
 void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st);
-void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st, bool tight = false);
+void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st, int tight = 0);
 // P2G adjoint of substep f fused with the G2P adjoint of substep f-1
-void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st);
+void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st,
+                            int tight = 0);
 
 void launch_bin(const BinArgs& b, int n_blocks, int block, cudaStream_t st);
 int bin_scan_blocks(long long G);

@@ -25,8 +25,8 @@ namespace dstir {
 // ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
-template <int VARIANT, bool SVDJ>
-__global__ void __launch_bounds__(256) p2g_kernel(FwdArgs a) {
+template <int VARIANT, bool SVDJ, int MINB>
+__global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     if (threadIdx.x == 0) {
@@ -176,9 +176,6 @@ __global__ void __launch_bounds__(256) grid_kernel(FwdArgs a) {
     }
 }
 
-// MINB: minimum resident blocks per SM the register allocation must allow
-// (1: unconstrained; the "tight" option selects 4 for G2P and 3 for the
-// adjoint kernels, trading a few spilled registers for occupancy)
 template <int MINB>
 __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
     __shared__ SceneDev s;
@@ -274,8 +271,8 @@ __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
 // stress of substep f+1 (compute_F_tmp :39-42 with F[f+1] read back, p2g
 // :104-196), which scatters into the next grid.  Saves a pass over the
 // particle state and a launch per substep.
-template <int VARIANT, bool SVDJ>
-__global__ void __launch_bounds__(256) g2p_p2g_kernel(FwdArgs a) {
+template <int VARIANT, bool SVDJ, int MINB>
+__global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
@@ -670,8 +667,8 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
 // state adjoint of f (x, v, C parts) goes from the first half to the second
 // in registers; only its F part (read by the P2G adjoint of f-1) and the
 // position-adjoint part of f-1 are stored.
-template <int VARIANT, bool SVDJ>
-__global__ void __launch_bounds__(256) p2g_adj_g2p_adj_kernel(AdjArgs a) {
+template <int VARIANT, bool SVDJ, int MINB>
+__global__ void __launch_bounds__(256, MINB) p2g_adj_g2p_adj_kernel(AdjArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
@@ -871,74 +868,92 @@ __global__ void reduce_pgrad_kernel(const float* pgrad, int T, int B, float* out
 // ---------------------------------------------------------------------------
 // launchers
 // ---------------------------------------------------------------------------
-void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st) {
+// Launch bounds.  MINB, the resident blocks per SM that the register
+// allocation must allow, is set per kernel and per "tight" level: level 0
+// keeps the allocation the compiler picks for 256-thread blocks (64 registers
+// for P2G, 80 for G2P and the fused forward, about 110-130 for the
+// adjoints); level 1 caps G2P and the fused forward at 64 and the adjoints at
+// 80 registers (a few spilled bytes, half again as many resident warps);
+// level 2 also caps P2G at 48.
+void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;
+    const bool t2 = tight >= 2 && !svdj;
     if (variant == P2G_PLAIN)
-        svdj ? p2g_kernel<P2G_PLAIN, true><<<n_blocks, block, 0, st>>>(a)
-             : p2g_kernel<P2G_PLAIN, false><<<n_blocks, block, 0, st>>>(a);
+        svdj ? p2g_kernel<P2G_PLAIN, true, 4><<<n_blocks, block, 0, st>>>(a)
+             : p2g_kernel<P2G_PLAIN, false, 4><<<n_blocks, block, 0, st>>>(a);
     else if (variant == P2G_WARP)
-        svdj ? p2g_kernel<P2G_WARP, true><<<n_blocks, block, 0, st>>>(a)
-             : p2g_kernel<P2G_WARP, false><<<n_blocks, block, 0, st>>>(a);
+        svdj ? p2g_kernel<P2G_WARP, true, 4><<<n_blocks, block, 0, st>>>(a)
+        : t2 ? p2g_kernel<P2G_WARP, false, 5><<<n_blocks, block, 0, st>>>(a)
+             : p2g_kernel<P2G_WARP, false, 4><<<n_blocks, block, 0, st>>>(a);
     else
-        svdj ? p2g_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
-             : p2g_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
+        svdj ? p2g_kernel<P2G_VEC, true, 4><<<n_blocks, block, 0, st>>>(a)
+        : t2 ? p2g_kernel<P2G_VEC, false, 5><<<n_blocks, block, 0, st>>>(a)
+             : p2g_kernel<P2G_VEC, false, 4><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks > 0) grid_kernel<<<n_gblocks, gblock, 0, st>>>(a);
 }
-void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, bool tight) {
+void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;
-    if (tight)
+    if (tight >= 1)
         g2p_kernel<4><<<n_blocks, block, 0, st>>>(a);
     else
-        g2p_kernel<1><<<n_blocks, block, 0, st>>>(a);
+        g2p_kernel<3><<<n_blocks, block, 0, st>>>(a);
 }
-void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st) {
+void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;
+    const bool t1 = tight >= 1;
     if (variant == P2G_PLAIN)
-        svdj ? g2p_p2g_kernel<P2G_PLAIN, true><<<n_blocks, block, 0, st>>>(a)
-             : g2p_p2g_kernel<P2G_PLAIN, false><<<n_blocks, block, 0, st>>>(a);
+        svdj ? g2p_p2g_kernel<P2G_PLAIN, true, 3><<<n_blocks, block, 0, st>>>(a)
+             : g2p_p2g_kernel<P2G_PLAIN, false, 3><<<n_blocks, block, 0, st>>>(a);
     else if (variant == P2G_WARP)
-        svdj ? g2p_p2g_kernel<P2G_WARP, true><<<n_blocks, block, 0, st>>>(a)
-             : g2p_p2g_kernel<P2G_WARP, false><<<n_blocks, block, 0, st>>>(a);
+        svdj ? g2p_p2g_kernel<P2G_WARP, true, 3><<<n_blocks, block, 0, st>>>(a)
+        : t1 ? g2p_p2g_kernel<P2G_WARP, false, 4><<<n_blocks, block, 0, st>>>(a)
+             : g2p_p2g_kernel<P2G_WARP, false, 3><<<n_blocks, block, 0, st>>>(a);
     else
-        svdj ? g2p_p2g_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
-             : g2p_p2g_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
+        svdj ? g2p_p2g_kernel<P2G_VEC, true, 3><<<n_blocks, block, 0, st>>>(a)
+        : t1 ? g2p_p2g_kernel<P2G_VEC, false, 4><<<n_blocks, block, 0, st>>>(a)
+             : g2p_p2g_kernel<P2G_VEC, false, 3><<<n_blocks, block, 0, st>>>(a);
 }
-void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st, bool tight) {
+void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;
+    const bool t1 = tight >= 1;
     if (variant == P2G_PLAIN)
-        g2p_adj_kernel<P2G_PLAIN, 1><<<n_blocks, block, 0, st>>>(a);
+        g2p_adj_kernel<P2G_PLAIN, 2><<<n_blocks, block, 0, st>>>(a);
     else if (variant == P2G_WARP)
-        tight ? g2p_adj_kernel<P2G_WARP, 3><<<n_blocks, block, 0, st>>>(a)
-              : g2p_adj_kernel<P2G_WARP, 1><<<n_blocks, block, 0, st>>>(a);
+        t1 ? g2p_adj_kernel<P2G_WARP, 3><<<n_blocks, block, 0, st>>>(a)
+           : g2p_adj_kernel<P2G_WARP, 2><<<n_blocks, block, 0, st>>>(a);
     else
-        tight ? g2p_adj_kernel<P2G_VEC, 3><<<n_blocks, block, 0, st>>>(a)
-              : g2p_adj_kernel<P2G_VEC, 1><<<n_blocks, block, 0, st>>>(a);
+        t1 ? g2p_adj_kernel<P2G_VEC, 3><<<n_blocks, block, 0, st>>>(a)
+           : g2p_adj_kernel<P2G_VEC, 2><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks > 0) grid_adj_kernel<<<n_gblocks, gblock, 0, st>>>(a);
 }
-void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st, bool tight) {
+void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;
     if (svdj)
-        p2g_adj_kernel<true, 1><<<n_blocks, block, 0, st>>>(a);
-    else if (tight)
+        p2g_adj_kernel<true, 2><<<n_blocks, block, 0, st>>>(a);
+    else if (tight >= 1)
         p2g_adj_kernel<false, 3><<<n_blocks, block, 0, st>>>(a);
     else
-        p2g_adj_kernel<false, 1><<<n_blocks, block, 0, st>>>(a);
+        p2g_adj_kernel<false, 2><<<n_blocks, block, 0, st>>>(a);
 }
-void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st) {
+void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st,
+                            int tight) {
     if (n_blocks <= 0) return;
+    const bool t1 = tight >= 1;
     if (variant == P2G_PLAIN)
-        svdj ? p2g_adj_g2p_adj_kernel<P2G_PLAIN, true><<<n_blocks, block, 0, st>>>(a)
-             : p2g_adj_g2p_adj_kernel<P2G_PLAIN, false><<<n_blocks, block, 0, st>>>(a);
+        svdj ? p2g_adj_g2p_adj_kernel<P2G_PLAIN, true, 2><<<n_blocks, block, 0, st>>>(a)
+             : p2g_adj_g2p_adj_kernel<P2G_PLAIN, false, 2><<<n_blocks, block, 0, st>>>(a);
     else if (variant == P2G_WARP)
-        svdj ? p2g_adj_g2p_adj_kernel<P2G_WARP, true><<<n_blocks, block, 0, st>>>(a)
-             : p2g_adj_g2p_adj_kernel<P2G_WARP, false><<<n_blocks, block, 0, st>>>(a);
+        svdj ? p2g_adj_g2p_adj_kernel<P2G_WARP, true, 2><<<n_blocks, block, 0, st>>>(a)
+        : t1 ? p2g_adj_g2p_adj_kernel<P2G_WARP, false, 3><<<n_blocks, block, 0, st>>>(a)
+             : p2g_adj_g2p_adj_kernel<P2G_WARP, false, 2><<<n_blocks, block, 0, st>>>(a);
     else
-        svdj ? p2g_adj_g2p_adj_kernel<P2G_VEC, true><<<n_blocks, block, 0, st>>>(a)
-             : p2g_adj_g2p_adj_kernel<P2G_VEC, false><<<n_blocks, block, 0, st>>>(a);
+        svdj ? p2g_adj_g2p_adj_kernel<P2G_VEC, true, 2><<<n_blocks, block, 0, st>>>(a)
+        : t1 ? p2g_adj_g2p_adj_kernel<P2G_VEC, false, 3><<<n_blocks, block, 0, st>>>(a)
+             : p2g_adj_g2p_adj_kernel<P2G_VEC, false, 2><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
                        long long stride, long long n, cudaStream_t s) {

@@ -68,10 +68,11 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 0, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 2}, {'p2g': 3},
             {'p2g': 3, 'brick_scatter': 0}, {'p2g': 3, 'brick_scatter': 2}, {'p2g': 3, 'brick_gather': 0},
             {'p2g': 3, 'graph': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 4, 'resort': 0},
-            {'p2g': 4, 'graph': 1}, {'p2g': 4, 'tight': 1}]
+            {'p2g': 4, 'graph': 1}, {'p2g': 4, 'tight': 0}, {'p2g': 4, 'tight': 2},
+            {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'tight': 0}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
-               'warp-tight']
+               'warp-tight0', 'warp-tight2', 'warp-fused-tight0']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
