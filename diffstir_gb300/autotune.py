@@ -46,7 +46,7 @@ def shape_key(scenes):
     rod = scenes[0].desc.rod_mode
     svd = int(any(s.desc.j_mode == 1 for s in scenes))
     name = torch.cuda.get_device_name() if torch.cuda.is_available() else 'cpu'
-    return 'v5|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
+    return 'v6|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
 
 
 def _load():
@@ -89,12 +89,20 @@ def time_config(scenes, options, nsteps, ckpt, reps=2):
     return e0.elapsed_time(e1) / 1e3 / reps
 
 
-def autotune(scenes, nsteps=40, ckpt=20, candidates=None, use_cache=True, verbose=False):
-    """Best options dict for ``scenes`` (a Scene or a list)."""
+def autotune(scenes, nsteps=200, ckpt=50, candidates=None, use_cache=True, verbose=False):
+    """Best options dict for ``scenes`` (a Scene or a list).
+
+    Each candidate times a recorded forward + adjoint of ``nsteps`` substeps.
+    The horizon spans several checkpoint segments: the particle order, and
+    with it the scatter cost, degrades between re-sorts, so a short run from
+    the freshly sorted initial state would favour the wrong kernels."""
     key = shape_key(scenes)
     cache = _load() if use_cache else {}
     if key in cache:
         return dict(cache[key]['options'])
+    lst = scenes if isinstance(scenes, (list, tuple)) else [scenes]
+    nsteps = max(1, min(nsteps, max(s.n_steps for s in lst)))
+    ckpt = min(ckpt, nsteps)
     results = []
     for opt in (candidates or CANDIDATES):
         t0 = time.perf_counter()
