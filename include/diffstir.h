@@ -116,7 +116,9 @@ int dstir_set_trajectory(DstirHandle* h, const float* traj, void* stream);
  * trajectory entries).  force_out [batch, nsteps, 3] receives the rod reaction
  * force of each substep: entry f is the reference's force at frame t0+f+1
  * (compute_loss, :330-339).  With record != 0 the state is checkpointed every
- * `ckpt_every` substeps for dstir_backward.  Replaces forward(s), :341-348. */
+ * `ckpt_every` substeps for dstir_backward.  With the "resort" option on, the
+ * particle order is rebuilt every `ckpt_every` substeps, recorded or not
+ * (ckpt_every <= 0 without record: never).  Replaces forward(s), :341-348. */
 int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every,
                   int32_t record, float* force_out, void* stream);
 
@@ -138,17 +140,21 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams,
  * gradient_descent_module.py:51-54.) */
 int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
 
-/* Tuning knobs: "p2g" (0 scalar atomics per particle, 1 vector atomics per
- * particle, 2 cell-binned one-thread-per-cell accumulation, 3 brick-binned
- * shared-memory tiles with one CTA per 4x4x4-cell brick, 4 vector atomics
- * after summing neighbouring lanes' contributions to shared stencil nodes by
- * warp shuffles; 2, 3 and 4 also select the matching G2P-adjoint scatter),
- * "block" / "gblock" (threads per particle / grid block: 64, 128 or 256),
- * "graph" (1: replay each rollout and each reverse pass as a cached CUDA
- * graph), "fuse" / "fuse_adj" (1: G2P of substep f fused with P2G of f+1 /
- * P2G adjoint of f fused with the G2P adjoint of f-1), "brick_scatter" /
- * "brick_gather" (scatter and gather forms of variant 3), "profile" (1: time
- * every launch with CUDA events; totals via dstir_get_option
+/* Tuning knobs (defaults in brackets): "p2g" [4] (0 scalar atomics per
+ * particle, 1 vector atomics per particle, 2 cell-binned one-thread-per-cell
+ * accumulation, 3 brick-binned shared-memory tiles with one CTA per
+ * 4x4x4-cell brick, 4 vector atomics after summing neighbouring lanes'
+ * contributions to shared stencil nodes by warp shuffles; 2, 3 and 4 also
+ * select the matching G2P-adjoint scatter), "block" / "gblock" [256]
+ * (threads per particle / grid block: 64, 128 or 256), "graph" [0] (1:
+ * replay each rollout and each reverse pass as a cached CUDA graph), "fuse" /
+ * "fuse_adj" [0] (1: G2P of substep f fused with P2G of f+1 / P2G adjoint of
+ * f fused with the G2P adjoint of f-1), "resort" [1] (re-sort the particle
+ * order every ckpt_every substeps of a rollout; states and state adjoints
+ * still cross the ABI in the order given to dstir_set_state), "tight" [1]
+ * (register-cap level of the particle kernels, 0..2), "brick_scatter" /
+ * "brick_gather" (scatter and gather forms of variant 3), "profile" [0] (1:
+ * time every launch with CUDA events; totals via dstir_get_option
  * "prof_ns:<kernel>" / "prof_count:<kernel>"), "launches" (reset the launch
  * counter). */
 int dstir_set_option(DstirHandle* h, const char* key, int64_t value);
