@@ -45,12 +45,15 @@ def load():
         D = C.POINTER(C.c_double)
         sig_roll = [C.POINTER(DstirSceneDesc), D, D, C.c_int, D, D, D, D, D, D, C.c_int]
         sig_grad = [C.POINTER(DstirSceneDesc), D, D, C.c_int, D, D, D, D, D, D, D, D, C.c_int]
-        for name in ('oracle_rollout_f64', 'oracle_rollout_f32'):
+        for name in ('oracle_rollout_f64', 'oracle_rollout_f32', 'oracle_rollout_last_f64'):
             getattr(lib, name).argtypes = sig_roll
             getattr(lib, name).restype = C.c_int
         for name in ('oracle_grad_f64', 'oracle_grad_f32'):
             getattr(lib, name).argtypes = sig_grad
             getattr(lib, name).restype = C.c_int
+        lib.oracle_grad_seeded_f64.argtypes = [C.POINTER(DstirSceneDesc), D, D, C.c_int, D, D, D, D, D, D, D, D,
+                                               D, C.c_int]
+        lib.oracle_grad_seeded_f64.restype = C.c_int
         lib.oracle_svd3_f64.argtypes = [D, D, D, D, C.c_int64]
         lib.oracle_svd3_f64.restype = None
         lib.oracle_svd3_backward_f64.argtypes = [D, D, D, D, D, D, D, C.c_int64]
@@ -106,6 +109,43 @@ def grad(desc, params, traj, T, x0, dL_dforce, v0=None, C0=None, F0=None, precis
     fn = lib.oracle_grad_f64 if precision == 'f64' else lib.oracle_grad_f32
     rc = fn(C.byref(desc), _p(params), _p(traj), T, _p(x0), _p(v0), _p(C0), _p(F0),
             _p(dL), _p(force), _p(dp), _p(ds), threads)
+    if rc < 0:
+        raise RuntimeError('oracle grad failed: %d' % rc)
+    return force, dp, ds, rc
+
+
+def rollout_last(desc, params, traj, T, x0, v0=None, C0=None, F0=None, threads=1):
+    """FP64 rollout returning (force [T,3], final state [N,24], status); keeps
+    only the states of this call, so long rollouts run as chained segments."""
+    lib = load()
+    N = desc.n_liquid + desc.n_rod + desc.n_container
+    params, traj = _arr(params), _arr(traj)
+    x0, v0, C0, F0 = _arr(x0), _arr(v0), _arr(C0), _arr(F0)
+    force = np.zeros((T, 3))
+    last = np.zeros((N, 24))
+    rc = lib.oracle_rollout_last_f64(C.byref(desc), _p(params), _p(traj), T, _p(x0), _p(v0), _p(C0), _p(F0),
+                                     _p(force), _p(last), threads)
+    if rc < 0:
+        raise RuntimeError('oracle rollout failed: %d' % rc)
+    return force, last, rc
+
+
+def grad_seeded(desc, params, traj, T, x0, dL_dforce, dL_dstateT=None, v0=None, C0=None, F0=None, threads=1):
+    """FP64 rollout + reverse pass seeded with the adjoint of the final state
+    [N,24] (None: zero); returns (force, dL_dparams[4], dL_dstate0 [N,24],
+    status).  Chaining it backwards over segments gives the gradient of a
+    rollout whose states do not fit in memory at once."""
+    lib = load()
+    N = desc.n_liquid + desc.n_rod + desc.n_container
+    params, traj = _arr(params), _arr(traj)
+    x0, v0, C0, F0 = _arr(x0), _arr(v0), _arr(C0), _arr(F0)
+    dL = _arr(dL_dforce, (T, 3))
+    seed = None if dL_dstateT is None else _arr(dL_dstateT, (N, 24))
+    force = np.zeros((T, 3))
+    dp = np.zeros(4)
+    ds = np.zeros((N, 24))
+    rc = lib.oracle_grad_seeded_f64(C.byref(desc), _p(params), _p(traj), T, _p(x0), _p(v0), _p(C0), _p(F0),
+                                    _p(dL), _p(seed), _p(force), _p(dp), _p(ds), threads)
     if rc < 0:
         raise RuntimeError('oracle grad failed: %d' % rc)
     return force, dp, ds, rc

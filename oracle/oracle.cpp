@@ -597,8 +597,13 @@ struct Sim {
     std::vector<R> gpm;                // G*4 P/M adjoint
     double dprm[4] = {0, 0, 0, 0};
 
-    void backward(const double* dL_dforce, double* dL_dparams, double* dL_dstate0) {
+    // dL_dstateT (optional): adjoint of the final state, for chaining the
+    // reverse pass over consecutive segments of a long rollout
+    void backward(const double* dL_dforce, double* dL_dparams, double* dL_dstate0,
+                  const double* dL_dstateT = nullptr) {
         adj_next.assign((size_t)N * NS, R(0));
+        if (dL_dstateT)
+            for (size_t i = 0; i < (size_t)N * NS; ++i) adj_next[i] = R(dL_dstateT[i]);
         adj_cur.assign((size_t)N * NS, R(0));
         gadj.assign((size_t)G * 4, R(0));
         gpm.assign((size_t)G * 4, R(0));
@@ -916,7 +921,8 @@ template <class R>
 int rollout_impl(const DstirSceneDesc* d, const double* params, const double* traj, int T,
                  const double* x0, const double* v0, const double* C0, const double* F0,
                  double* force_out, double* states_out, int threads, const double* dL_dforce,
-                 double* dL_dparams, double* dL_dstate0) {
+                 double* dL_dparams, double* dL_dstate0, const double* dL_dstateT = nullptr,
+                 double* last_out = nullptr) {
     if (!d || !params || !traj || !x0 || T < 0) return DSTIR_EINVAL;
     if (d->n_grid < 4) return DSTIR_EINVAL;
     Sim<R> sim(*d, params, traj, T, threads);
@@ -926,7 +932,9 @@ int rollout_impl(const DstirSceneDesc* d, const double* params, const double* tr
         for (size_t i = 0; i < (size_t)T * 3; ++i) force_out[i] = (double)sim.force[i];
     if (states_out)
         for (size_t i = 0; i < sim.st.size(); ++i) states_out[i] = (double)sim.st[i];
-    if (dL_dforce) sim.backward(dL_dforce, dL_dparams, dL_dstate0);
+    if (last_out)
+        for (size_t i = 0; i < (size_t)sim.N * NS; ++i) last_out[i] = (double)sim.st[(size_t)T * sim.N * NS + i];
+    if (dL_dforce) sim.backward(dL_dforce, dL_dparams, dL_dstate0, dL_dstateT);
     return (int)status;
 }
 
@@ -965,6 +973,24 @@ int oracle_grad_f32(const DstirSceneDesc* d, const double* params, const double*
     if (!dL_dforce || !dL_dparams) return DSTIR_EINVAL;
     return rollout_impl<float>(d, params, traj, T, x0, v0, C0, F0, force_out, nullptr, threads,
                                dL_dforce, dL_dparams, dL_dstate0);
+}
+
+// Segment forms for rollouts too long to keep every state: the rollout
+// returns only its final state [N,24]; the reverse pass also takes the
+// adjoint of the final state [N,24] (NULL: zero).
+int oracle_rollout_last_f64(const DstirSceneDesc* d, const double* params, const double* traj, int T,
+                            const double* x0, const double* v0, const double* C0, const double* F0,
+                            double* force_out, double* last_out, int threads) {
+    return rollout_impl<double>(d, params, traj, T, x0, v0, C0, F0, force_out, nullptr, threads, nullptr,
+                                nullptr, nullptr, nullptr, last_out);
+}
+int oracle_grad_seeded_f64(const DstirSceneDesc* d, const double* params, const double* traj, int T,
+                           const double* x0, const double* v0, const double* C0, const double* F0,
+                           const double* dL_dforce, const double* dL_dstateT, double* force_out,
+                           double* dL_dparams, double* dL_dstate0, int threads) {
+    if (!dL_dforce || !dL_dparams) return DSTIR_EINVAL;
+    return rollout_impl<double>(d, params, traj, T, x0, v0, C0, F0, force_out, nullptr, threads, dL_dforce,
+                                dL_dparams, dL_dstate0, dL_dstateT);
 }
 
 void oracle_svd3_f64(const double* A, double* U, double* S, double* V, int64_t n) {

@@ -120,3 +120,31 @@ def test_svd3_backward_fd():
                 L = lambda u, s, v: (gU[n] * u[0]).sum() + (gS[n] * s[0]).sum() + (gV[n] * v[0]).sum()
                 fd = (L(Up, Sp, Vp) - L(Um, Sm, Vm)) / (2 * h)
                 assert abs(gA[n, i, j] - fd) < 1e-5 * max(1.0, abs(fd)), (n, i, j, gA[n, i, j], fd)
+
+
+def test_segment_chaining_equals_one_shot():
+    """The segment forms (rollout returning the last state, reverse pass
+    seeded with the adjoint of the final state) chained over four segments
+    reproduce the one-shot FP64 rollout and gradient."""
+    T, K = 40, 10
+    sc = S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=3)
+    w = np.random.default_rng(0).normal(size=(T, 3))
+    f1, dp1, ds1, _ = oracle.grad(sc.desc, sc.params, sc.trajectory, T, sc.x0(), w, want_state0=True)
+    state = (sc.x0(), None, None, None)
+    ckpts, forces = [], []
+    for s0 in range(0, T, K):
+        ckpts.append(state)
+        f, last, st = oracle.rollout_last(sc.desc, sc.params, sc.trajectory[s0:s0 + K + 1], K, *state)
+        assert st == 0
+        forces.append(f)
+        state = (last[:, 0:3], last[:, 3:6], last[:, 6:15], last[:, 15:24])
+    np.testing.assert_allclose(np.concatenate(forces), f1, rtol=0, atol=1e-12 * np.abs(f1).max())
+    adj, dp = None, np.zeros(4)
+    for i in reversed(range(len(ckpts))):
+        s0 = i * K
+        x, v, C, F = ckpts[i]
+        _, d, adj, _ = oracle.grad_seeded(sc.desc, sc.params, sc.trajectory[s0:s0 + K + 1], K, x, w[s0:s0 + K], adj,
+                                          v, C, F)
+        dp += d
+    np.testing.assert_allclose(dp, dp1, rtol=1e-12, atol=1e-14)
+    np.testing.assert_allclose(adj, ds1, rtol=1e-12, atol=1e-14)
