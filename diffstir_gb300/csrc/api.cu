@@ -139,6 +139,7 @@ struct DstirHandle {
     long long partial_len = 0;
     unsigned* counters = nullptr;
     unsigned* status = nullptr;
+    int* box = nullptr;              // [max_steps][B][6] occupied node box of each substep
 
     // per-substep binning (p2g variant P2G_CELL); one (cell_start, perm) slot per
     // substep of a segment, so the reverse pass reuses the recompute's bins
@@ -161,6 +162,7 @@ struct DstirHandle {
     // substeps of a rollout, at the checkpoint boundaries of a recorded one
     int resort = 1;             // option "resort": 0 never
     int tight = 1;              // option "tight": register-cap level of the particle kernels (0, 1, 2)
+    int use_box = 1;            // option "box": the grid kernels skip nodes outside the occupied box
     int max_n = 0;              // largest n_grid of the batch
     int* rs_cnt = nullptr;      // [G+1]
     int* rs_start = nullptr;    // [G+2]
@@ -359,6 +361,19 @@ int ensure_bin_slots(DstirHandle* h, long long n) {
 
 bool binned(const DstirHandle* h) { return h->p2g_variant == P2G_CELL || h->p2g_variant == P2G_BRICK; }
 
+// Occupied-box slot of relative substep k (NULL for the binned variants,
+// whose scatter kernels do not track the box: their grid update covers every
+// node).
+int* box_slot(DstirHandle* h, long long k) {
+    if (!h->use_box || binned(h) || k < 0 || k >= h->max_steps) return nullptr;
+    return h->box + (size_t)k * h->B * 6;
+}
+
+void reset_boxes(DstirHandle* h, long long k0, long long n, cudaStream_t st) {
+    if (!h->use_box || binned(h) || n <= 0) return;
+    cudaMemsetAsync(h->box + (size_t)k0 * h->B * 6, 0x80, (size_t)n * h->B * 6 * sizeof(int), st);
+}
+
 int* slot_cell_start(DstirHandle* h, int slot) { return h->cell_start + (size_t)slot * (h->nbins_max + 2); }
 int* slot_perm(DstirHandle* h, int slot) { return h->perm + (size_t)slot * h->stride; }
 
@@ -529,6 +544,7 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
         (rc = dalloc(h, &h->pgrad, (size_t)max_steps * batch * 4, "parameter gradients")) ||
         (rc = dalloc(h, &h->counters, (size_t)3 * batch, "counters")) ||
         (rc = dalloc(h, &h->status, 1, "status")) || (rc = dalloc(h, &h->bricks, h->bricks_h.size(), "bricks")) ||
+        (rc = dalloc(h, &h->box, (size_t)max_steps * batch * 6, "occupied boxes")) ||
         (rc = dalloc(h, &h->perm_cur, (size_t)h->stride, "particle order")) ||
         (rc = dalloc(h, &h->perm_tmp, (size_t)h->stride, "particle order")) ||
         (rc = dalloc(h, &h->perm_rec0, (size_t)h->stride, "particle order")) ||
@@ -575,7 +591,7 @@ void dstir_destroy(DstirHandle* h) {
                     h->traj, h->params, h->models, h->force_scratch, h->pgrad, h->partial, h->counters, h->status,
                     h->cnt, h->bkey, h->brank, h->bsum, h->cell_start, h->perm, h->fbuf, h->dfbuf, h->dpbuf,
                     h->bricks, h->rs_cnt, h->rs_start, h->rs_bsum, h->rs_key, h->rs_rank, h->rs_sorted,
-                    h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0};
+                    h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0, h->box};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -648,12 +664,15 @@ bool fused_adj(const DstirHandle* h) { return h->fuse_adj && !binned(h); }
 template <class SlotFn, class GridFn>
 void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids, float* force,
                    long long fstride, int fo0, int clear_pm, bool skip_last_g2p, bool per_step_bins,
-                   cudaStream_t st) {
+                   int box0, cudaStream_t st) {
+    // box0: occupied-box slot of substep 0 of this chain
+    reset_boxes(h, box0, nsteps, st);
     if (!fused(h)) {
         for (int k = 0; k < nsteps; ++k) {
             float4 *pm, *vo;
             grids(k, pm, vo);
             FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + k, force, fstride, fo0 + k, clear_pm);
+            a.box = box_slot(h, box0 + k);
             run_substep(h, a, st, per_step_bins ? k : 0);
         }
         return;
@@ -662,18 +681,21 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
         float4 *pm, *vo;
         grids(0, pm, vo);
         FwdArgs a = fwd_args(h, slot(0), slot(1), pm, vo, t0, force, fstride, fo0, clear_pm);
+        a.box = box_slot(h, box0);
         timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st, h->tight); });
     }
     for (int k = 0; k < nsteps; ++k) {
         float4 *pm, *vo;
         grids(k, pm, vo);
         FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + k, force, fstride, fo0 + k, clear_pm);
+        a.box = box_slot(h, box0 + k);
         timed(h, K_GRID, st, [&] { launch_grid(a, h->n_gblocks, h->gblock, st); });
         if (k + 1 < nsteps) {
             float4 *pmn, *von;
             grids(k + 1, pmn, von);
             a.next2 = slot(k + 2);
             a.pm_next = pmn;
+            a.box_next = box_slot(h, box0 + k + 1);
             timed(h, K_G2P_P2G, st,
                   [&] { launch_g2p_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st, h->tight); });
         } else if (!skip_last_g2p) {
@@ -771,7 +793,7 @@ int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, cuda
             if (record && k % K == 0 && k < nsteps) return h->ckpt + (size_t)(k / K) * sf;
             return W[(cur + k) % 3];
         };
-        chain_forward(h, t0, nsteps, slot, grids, h->fbuf, (long long)h->max_steps * 3, 0, 1, false, false, st);
+        chain_forward(h, t0, nsteps, slot, grids, h->fbuf, (long long)h->max_steps * 3, 0, 1, false, false, 0, st);
         return (cur + nsteps) % 3;
     }
     int a = cur;
@@ -779,7 +801,7 @@ int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, cuda
     for (int c = 0, k0 = 0;; ++c) {
         const int L = std::min(K, nsteps - k0);
         auto slot = [&](int j) -> float* { return j == 0 ? in : W[(a + j) % 3]; };
-        chain_forward(h, t0 + k0, L, slot, grids, h->fbuf, (long long)h->max_steps * 3, k0, 1, false, false, st);
+        chain_forward(h, t0 + k0, L, slot, grids, h->fbuf, (long long)h->max_steps * 3, k0, 1, false, false, k0, st);
         const int out = (a + L) % 3;
         if (k0 + L >= nsteps) return out;
         float* next = record ? h->ckpt + (size_t)(c + 1) * sf : W[(out + 1) % 3];
@@ -894,6 +916,8 @@ int dstir_substep(DstirHandle* h, int32_t f, float* force_out, void* stream) {
     long long fstride = force_out ? 3 : (long long)h->max_steps * 3;
     int fo = force_out ? 0 : f;
     FwdArgs a = fwd_args(h, W[h->cur], W[(h->cur + 1) % 3], h->pm, h->vo, f, force, fstride, fo, 1);
+    reset_boxes(h, 0, 1, st);
+    a.box = box_slot(h, 0);
     run_substep(h, a, st);
     CUDA_TRY(h, cudaGetLastError());
     h->cur = (h->cur + 1) % 3;
@@ -928,7 +952,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
         // recompute the segment, keeping every state and grid; the state after
         // its last substep is not needed by the adjoint
         chain_forward(h, t0 + s0, L, slot, grids, h->force_scratch, (long long)h->max_steps * 3, t0 + s0, 0, true,
-                      true, st);
+                      true, s0, st);
         // adjoint of the state at global step g (relative to t0) lives in A[(n - g) & 1]
         auto adj_args = [&](int k) {
             AdjArgs a;
@@ -958,6 +982,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.cur2 = nullptr;
             a.vo2 = nullptr;
             a.adj_prev = nullptr;
+            a.box = box_slot(h, s0 + k);
             return a;
         };
         if (!fused_adj(h)) {
@@ -1080,6 +1105,12 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         h->recorded = false;
         return DSTIR_OK;
     }
+    if (!strcmp(key, "box")) {
+        h->use_box = value ? 1 : 0;
+        ++h->epoch;
+        h->recorded = false;
+        return DSTIR_OK;
+    }
     if (!strcmp(key, "tight")) {
         if (value < 0 || value > 2) return fail(h, DSTIR_EINVAL, "tight %lld not in 0..2", (long long)value);
         h->tight = (int)value;
@@ -1135,6 +1166,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "fuse_adj")) *value = h->fuse_adj;
     else if (!strcmp(key, "resort")) *value = h->resort;
     else if (!strcmp(key, "tight")) *value = h->tight;
+    else if (!strcmp(key, "box")) *value = h->use_box;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

@@ -5,6 +5,8 @@
 
 #include <cuda_runtime.h>
 
+#include <climits>
+
 #include "common.cuh"
 #include "svd.cuh"
 
@@ -147,6 +149,42 @@ __device__ __forceinline__ void run_agg_scatter(const RunAgg& r, float4* row, fl
         atomicAdd(row + 1, c1);
         atomicAdd(row + 2, c2);
     }
+}
+
+// ---------------------------------------------------------------------------
+// occupied node box of a scene
+//
+// box[0..2] = -(lowest stencil node index) per axis, box[3..5] = highest, all
+// maximised with atomicMax from the reset value 0x80808080 (INT_MIN-like), so
+// one byte memset empties a box.  A node (i, j, k) lies in the box when
+// -box[0] <= i <= box[3] and so on.  Block-wide: every thread of the block
+// must call box_update; one thread per block issues the atomics, and only for
+// bounds that the (possibly stale) current box does not already hold.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void box_update(int* box, const int base[3], bool valid, int (*sh)[6]) {
+    const unsigned full = 0xffffffffu;
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    int v[6];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        v[c] = valid ? -base[c] : INT_MIN;
+        v[3 + c] = valid ? base[c] + 2 : INT_MIN;
+    }
+#pragma unroll
+    for (int c = 0; c < 6; ++c) v[c] = __reduce_max_sync(full, v[c]);
+    if (lane == 0)
+#pragma unroll
+        for (int c = 0; c < 6; ++c) sh[w][c] = v[c];
+    __syncthreads();
+    if (threadIdx.x < 6) {
+        int m = INT_MIN;
+        for (int q = 0; q < (int)(blockDim.x >> 5); ++q) m = max(m, sh[q][threadIdx.x]);
+        if (m != INT_MIN && m > *(volatile int*)(box + threadIdx.x)) atomicMax(box + threadIdx.x, m);
+    }
+}
+
+__device__ __forceinline__ bool box_inside(const int* box, int i, int j, int k) {
+    return i >= -box[0] && j >= -box[1] && k >= -box[2] && i <= box[3] && j <= box[4] && k <= box[5];
 }
 
 // ---------------------------------------------------------------------------

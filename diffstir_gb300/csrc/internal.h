@@ -31,8 +31,14 @@ struct FwdArgs {
     int clear_pm;           // grid kernel zeroes pm after reading it
     int batch;
     // fused G2P(f) + P2G(f+1) only: F of state f+2 and the grid of substep f+1
-    float* next2;
-    float4* pm_next;
+    float* next2 = nullptr;
+    float4* pm_next = nullptr;
+    // occupied node box of each scene ([B][6]: -imin, -jmin, -kmin, imax, jmax,
+    // kmax, all maximised by atomicMax from 0x80808080): the P2G of this
+    // substep writes `box`, the fused P2G of the next one `box_next`; the grid
+    // update skips nodes outside `box`.  NULL: no box (every node is updated)
+    int* box = nullptr;
+    int* box_next = nullptr;
 };
 
 struct AdjArgs {
@@ -60,9 +66,10 @@ struct AdjArgs {
     unsigned* counters;
     int batch;
     // fused P2G adjoint of substep f with the G2P adjoint of substep f-1 only
-    const float* cur2;       // state at substep f-1
-    const float4* vo2;       // grid velocity of substep f-1
-    float* adj_prev;         // adjoint slot of state f-1 (receives its position-adjoint part)
+    const float* cur2 = nullptr;     // state at substep f-1
+    const float4* vo2 = nullptr;     // grid velocity of substep f-1
+    float* adj_prev = nullptr;       // adjoint slot of state f-1 (receives its position-adjoint part)
+    const int* box = nullptr;        // occupied node box of substep f (see FwdArgs::box) or NULL
 };
 
 // Counting sort of the particles of one substep by stencil-base cell.

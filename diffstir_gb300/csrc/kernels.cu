@@ -29,6 +29,7 @@ template <int VARIANT, bool SVDJ, int MINB>
 __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
+    __shared__ int boxsh[8][6];
     if (threadIdx.x == 0) {
         bi = a.blk[blockIdx.x];
         s = a.sc[bi.scene];
@@ -37,8 +38,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
     constexpr bool WARP = VARIANT == P2G_WARP;
     long long p = bi.start + threadIdx.x;
     bool active = p < bi.end;
-    if (!WARP && !active) return;
-    if (!active) p = bi.end - 1;  // WARP: the lane computes a copy and scatters nothing
+    if (!active) p = bi.end - 1;  // the lane computes a copy and writes nothing
     float x[3], v[3], C[9];
     load3(a.cur, a.stride, OX, p, x);
     load3(a.cur, a.stride, OV, p, v);
@@ -71,11 +71,11 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
     float fx[3];
     if (!locate(x, s.inv_dx, s.n, base, fx)) {
         if (active) atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
-        if (!WARP) return;
         active = false;
         base[0] = base[1] = base[2] = 0;
         fx[0] = fx[1] = fx[2] = 1.f;
     }
+    if (a.box) box_update(a.box + bi.scene * 6, base, active, boxsh);
     float w[3][3];
     bspline(fx, w);
     float mv[3] = {m * vv[0], m * vv[1], m * vv[2]};
@@ -99,13 +99,15 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
                 float gm = W * m;
                 float4* dst = a.pm + row + k;
                 if (VARIANT == P2G_PLAIN) {
-                    float* d = reinterpret_cast<float*>(dst);
-                    atomicAdd(d + 0, g0);
-                    atomicAdd(d + 1, g1);
-                    atomicAdd(d + 2, g2);
-                    atomicAdd(d + 3, gm);
+                    if (active) {
+                        float* d = reinterpret_cast<float*>(dst);
+                        atomicAdd(d + 0, g0);
+                        atomicAdd(d + 1, g1);
+                        atomicAdd(d + 2, g2);
+                        atomicAdd(d + 3, gm);
+                    }
                 } else if (VARIANT == P2G_VEC) {
-                    red_add4(dst, g0, g1, g2, gm);
+                    if (active) red_add4(dst, g0, g1, g2, gm);
                 } else {
                     c[k] = make_float4(g0, g1, g2, gm);
                 }
@@ -131,10 +133,12 @@ __global__ void __launch_bounds__(256) grid_kernel(FwdArgs a) {
     __syncthreads();
     long long node = gb.start + threadIdx.x;
     float fsum[3] = {0.f, 0.f, 0.f};
-    if (node < gb.end) {
-        long long local = node - s.goff;
-        int n = s.n;
-        int i = (int)(local / ((long long)n * n)), j = (int)((local / n) % n), k = (int)(local % n);
+    const long long local = node - s.goff;
+    const int n = s.n;
+    const int i = (int)(local / ((long long)n * n)), j = (int)((local / n) % n), k = (int)(local % n);
+    // nodes outside the occupied box hold no mass and no stencil reads them:
+    // their P2G entry is still zero and their velocity is never gathered
+    if (node < gb.end && (!a.box || box_inside(a.box + gb.scene * 6, i, j, k))) {
         float4 g = a.pm[node];
         if (a.clear_pm) a.pm[node] = make_float4(0.f, 0.f, 0.f, 0.f);
         float inv_m = 1.f / (g.w + 1e-10f);
@@ -279,6 +283,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
     __shared__ float tv[3];
     __shared__ float prm[4];
     __shared__ int model;
+    __shared__ int boxsh[8][6];
     if (threadIdx.x == 0) {
         bi = a.blk[blockIdx.x];
         s = a.sc[bi.scene];
@@ -291,9 +296,9 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
     constexpr bool WARP = VARIANT == P2G_WARP;
     long long p = bi.start + threadIdx.x;
     bool active = p < bi.end;
-    if (WARP && !active) p = bi.end - 1;  // the lane computes a copy and writes nothing
+    if (!active) p = bi.end - 1;  // the lane computes a copy and writes nothing
     float dv[3] = {0.f, 0.f, 0.f};
-    if (active || WARP) {
+    {
         // ---- G2P of substep f
         float x[3];
         load3(a.cur, a.stride, OX, p, x);
@@ -383,11 +388,12 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
         bool in2 = locate(x, s.inv_dx, s.n, base, fx);
         if (!in2 && active) atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
         bool act2 = active && in2;
-        if (WARP && !in2) {
+        if (!in2) {
             base[0] = base[1] = base[2] = 0;
             fx[0] = fx[1] = fx[2] = 1.f;
         }
-        if (in2 || WARP) {
+        if (a.box_next) box_update(a.box_next + bi.scene * 6, base, act2, boxsh);
+        {
             float w[3][3];
             bspline(fx, w);
             RunAgg ra;
@@ -410,13 +416,15 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
                         float gm = W * m;
                         float4* dst = a.pm_next + row + k;
                         if (VARIANT == P2G_PLAIN) {
-                            float* d = reinterpret_cast<float*>(dst);
-                            atomicAdd(d + 0, g0);
-                            atomicAdd(d + 1, g1);
-                            atomicAdd(d + 2, g2);
-                            atomicAdd(d + 3, gm);
+                            if (act2) {
+                                float* d = reinterpret_cast<float*>(dst);
+                                atomicAdd(d + 0, g0);
+                                atomicAdd(d + 1, g1);
+                                atomicAdd(d + 2, g2);
+                                atomicAdd(d + 3, gm);
+                            }
                         } else if (VARIANT == P2G_VEC) {
-                            red_add4(dst, g0, g1, g2, gm);
+                            if (act2) red_add4(dst, g0, g1, g2, gm);
                         } else {
                             c[k] = make_float4(g0, g1, g2, gm);
                         }
@@ -554,6 +562,9 @@ __global__ void __launch_bounds__(256) grid_adj_kernel(AdjArgs a) {
     long long local = node - s.goff;
     int n = s.n;
     int i = (int)(local / ((long long)n * n)), j = (int)((local / n) % n), k = (int)(local % n);
+    // outside the occupied box the velocity adjoint is zero (no stencil
+    // scattered there) and no stencil gathers the P/M adjoint
+    if (a.box && !box_inside(a.box + gb.scene * 6, i, j, k)) return;
     float4 g = a.pm[node];
     float4 vb4 = a.ga[node];
     a.ga[node] = make_float4(0.f, 0.f, 0.f, 0.f);

@@ -152,7 +152,9 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * f fused with the G2P adjoint of f-1), "resort" [1] (re-sort the particle
  * order every ckpt_every substeps of a rollout; states and state adjoints
  * still cross the ABI in the order given to dstir_set_state), "tight" [1]
- * (register-cap level of the particle kernels, 0..2), "brick_scatter" /
+ * (register-cap level of the particle kernels, 0..2), "box" [1] (P2G records
+ * each scene's occupied node box and the grid update and its adjoint skip the
+ * nodes outside it; per-particle variants only), "brick_scatter" /
  * "brick_gather" (scatter and gather forms of variant 3), "profile" [0] (1:
  * time every launch with CUDA events; totals via dstir_get_option
  * "prof_ns:<kernel>" / "prof_count:<kernel>"), "launches" (reset the launch

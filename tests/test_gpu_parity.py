@@ -177,6 +177,36 @@ def test_resort_matches_fixed_order(opts):
             assert rel(ds[k], ds0[k]) < 1e-3, k
 
 
+@pytest.mark.parametrize('opts', [{'p2g': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 0},
+                                  {'p2g': 4, 'graph': 1}], ids=['vec', 'warp', 'warp-fused', 'plain', 'warp-graph'])
+def test_box_skip_matches_full_grid(opts):
+    """Skipping the grid nodes outside each scene's occupied box leaves
+    forces, state and gradients as with the full grid update; two scenes of
+    different sizes, the second one re-sorted at every checkpoint."""
+    T, K = 36, 6
+    scenes = [rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=8)),
+              rounded(S.small_synthetic_scene(n_grid=24, ppc=4, n_steps=T, seed=9))]
+    wts = torch.as_tensor(np.random.default_rng(5).normal(size=(2, T, 3)), dtype=torch.float32, device='cuda')
+    out = {}
+    for box in (0, 1):
+        sim = Simulator(scenes, max_steps=T, options=dict(opts, box=box))
+        f = sim.forward(T, ckpt_every=K, record=True).cpu().numpy()
+        st = {k: v.cpu().numpy() for k, v in sim.get_state().items()}
+        dp, ds = sim.backward(wts, want_state0=True)
+        assert sim.status() == 0
+        fs = sim.substep(T - 1).cpu().numpy()   # the single-substep entry point too
+        out[box] = (f, st, dp.cpu().numpy(), {k: v.cpu().numpy() for k, v in ds.items()}, fs)
+        sim.close()
+    f0, st0, dp0, ds0, fs0 = out[0]
+    f1, st1, dp1, ds1, fs1 = out[1]
+    assert rel(f1, f0) < 1e-5
+    for k in 'xvCF':
+        assert rel(st1[k], st0[k]) < 1e-4, k
+        assert rel(ds1[k], ds0[k]) < 1e-3, k
+    assert rel(dp1, dp0) < 1e-4
+    assert rel(fs1, fs0) < 1e-4
+
+
 def test_checkpoint_interval_invariance():
     T = 24
     sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=4))
