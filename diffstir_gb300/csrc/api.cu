@@ -163,6 +163,10 @@ struct DstirHandle {
     int resort = 1;             // option "resort": 0 never
     int tight = 1;              // option "tight": register-cap level of the particle kernels (0, 1, 2)
     int use_box = 1;            // option "box": the grid kernels skip nodes outside the occupied box
+    int reorder = 10;           // option "reorder": processing order rebuilt every this many substeps (0: never)
+    int* vord = nullptr;        // [vord_slots][stride] processing orders (slot j: substeps [jR, (j+1)R) of a segment)
+    long long vord_slots = 0;
+    int* rs_vdest = nullptr;    // [stride] scratch of the processing-order build
     int max_n = 0;              // largest n_grid of the batch
     int* rs_cnt = nullptr;      // [G+1]
     int* rs_start = nullptr;    // [G+2]
@@ -591,7 +595,7 @@ void dstir_destroy(DstirHandle* h) {
                     h->traj, h->params, h->models, h->force_scratch, h->pgrad, h->partial, h->counters, h->status,
                     h->cnt, h->bkey, h->brank, h->bsum, h->cell_start, h->perm, h->fbuf, h->dfbuf, h->dpbuf,
                     h->bricks, h->rs_cnt, h->rs_start, h->rs_bsum, h->rs_key, h->rs_rank, h->rs_sorted,
-                    h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0, h->box};
+                    h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0, h->box, h->vord, h->rs_vdest};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -655,6 +659,9 @@ namespace {
 bool fused(const DstirHandle* h) { return h->fuse && !binned(h); }
 bool fused_adj(const DstirHandle* h) { return h->fuse_adj && !binned(h); }
 
+const int* vorder_slot(const DstirHandle* h, int k, bool per_step);
+void enqueue_vorder(DstirHandle* h, const float* state, int* order, cudaStream_t st);
+
 // Forward chain of `nsteps` substeps over the state slots slot(0..nsteps).
 // With fusion: P2G(0), then per substep k the grid update and G2P(k) fused
 // with P2G(k+1); the last substep ends with a plain G2P unless `skip_last_g2p`.
@@ -673,6 +680,10 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
             grids(k, pm, vo);
             FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + k, force, fstride, fo0 + k, clear_pm);
             a.box = box_slot(h, box0 + k);
+            // per_step_bins marks the segment recompute, whose orders the
+            // reverse pass reuses; a forward rollout keeps one order slot
+            a.order = vorder_slot(h, k, per_step_bins);
+            if (a.order && k % h->reorder == 0) enqueue_vorder(h, slot(k), const_cast<int*>(a.order), st);
             run_substep(h, a, st, per_step_bins ? k : 0);
         }
         return;
@@ -752,6 +763,51 @@ void enqueue_resort(DstirHandle* h, const float* in, float* out, int* dest, cuda
 // Number of re-sorts in a rollout of nsteps substeps, chunk length K.
 long long resort_count(const DstirHandle* h, int nsteps, int K) {
     return resort_on(h) && K > 0 && nsteps > K ? (nsteps - 1) / K : 0;
+}
+
+// The processing order is rebuilt every h->reorder substeps inside each chain
+// of the unfused per-particle path (the fused kernels run two substeps per
+// thread and keep the physical order).
+bool vorder_on(const DstirHandle* h) { return h->reorder > 0 && resort_on(h) && !fused(h) && !fused_adj(h); }
+
+int ensure_vorder(DstirHandle* h, int K) {
+    if (!vorder_on(h)) return DSTIR_OK;
+    int rc;
+    if ((rc = ensure_resort(h, 1))) return rc;
+    if (!h->rs_vdest && (rc = dalloc(h, &h->rs_vdest, (size_t)h->stride, "processing-order scratch"))) return rc;
+    long long slots = std::max<long long>(1, (K - 1) / h->reorder + 1);
+    if (slots > h->vord_slots) {
+        if ((rc = dalloc(h, &h->vord, (size_t)(slots * h->stride), "processing orders"))) return rc;
+        h->vord_slots = slots;
+    }
+    return DSTIR_OK;
+}
+
+// Processing order of substep k of a chain: NULL before the first rebuild.
+const int* vorder_slot(const DstirHandle* h, int k, bool per_step) {
+    if (!vorder_on(h) || k < h->reorder) return nullptr;
+    return h->vord + (size_t)(per_step ? k / h->reorder : 0) * h->stride;
+}
+
+void enqueue_vorder(DstirHandle* h, const float* state, int* order, cudaStream_t st) {
+    ResortArgs r;
+    r.sc = h->sc;
+    r.blk = h->blk;
+    r.in = state;
+    r.out = nullptr;
+    r.stride = h->stride;
+    r.cnt = h->rs_cnt;
+    r.cell_start = h->rs_start;
+    r.bsum = h->rs_bsum;
+    r.G = h->G;
+    r.key = h->rs_key;
+    r.rank = h->rs_rank;
+    r.sorted = h->rs_sorted;
+    r.dest = h->rs_vdest;
+    r.perm_in = nullptr;
+    r.perm_out = nullptr;
+    h->launches += 6;  // seven kernels; timed() counts one
+    timed(h, K_OTHER, st, [&] { launch_order(r, order, h->n_blocks, h->block, h->max_n, h->B, st); });
 }
 
 // Work slot that holds the final state of a forward rollout (the same
@@ -880,8 +936,10 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
     if (binned(h) && (rc = ensure_bin_slots(h, 1))) return rc;
     const long long nres = resort_count(h, nsteps, K);
     if (nres && (rc = ensure_resort(h, record ? nseg : 1))) return rc;
+    if ((rc = ensure_vorder(h, K))) return rc;
     long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch,
-                         h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0), h->block * 4096 + h->gblock};
+                         h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0) + (vorder_on(h) ? 512 * h->reorder : 0),
+                         h->block * 4096 + h->gblock};
     rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want,
                          [&](cudaStream_t s2) { enqueue_forward(h, t0, nsteps, K, record != 0, s2); });
     if (rc) return rc;
@@ -983,6 +1041,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.vo2 = nullptr;
             a.adj_prev = nullptr;
             a.box = box_slot(h, s0 + k);
+            a.order = vorder_slot(h, k, true);
             return a;
         };
         if (!fused_adj(h)) {
@@ -1045,12 +1104,13 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
     }
     if ((rc = ensure_grid_slots(h, K))) return rc;
     if (binned(h) && (rc = ensure_bin_slots(h, K))) return rc;
+    if ((rc = ensure_vorder(h, K))) return rc;
     // dL/dforce [B][n][3] -> internal [B][max_steps][3]
     CUDA_TRY(h, cudaMemcpy2DAsync(h->dfbuf, (size_t)h->max_steps * 3 * sizeof(float), dL_dforce,
                                   (size_t)n * 3 * sizeof(float), (size_t)n * 3 * sizeof(float), (size_t)h->B,
                                   cudaMemcpyDeviceToDevice, st));
     long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant * 16 + h->fuse * 2 + h->fuse_adj,
-                         h->block * 4096 + h->gblock, h->rec_resort ? 1 : 0, 0};
+                         h->block * 4096 + h->gblock, h->rec_resort ? 1 : 0, vorder_on(h) ? h->reorder : 0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, [&](cudaStream_t s2) { enqueue_backward(h, s2); });
     if (rc) return rc;
@@ -1102,6 +1162,13 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     }
     if (!strcmp(key, "resort")) {
         h->resort = value ? 1 : 0;
+        h->recorded = false;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "reorder")) {
+        if (value < 0 || value > 1000000) return fail(h, DSTIR_EINVAL, "reorder %lld out of range", (long long)value);
+        h->reorder = (int)value;
+        ++h->epoch;
         h->recorded = false;
         return DSTIR_OK;
     }
@@ -1167,6 +1234,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "resort")) *value = h->resort;
     else if (!strcmp(key, "tight")) *value = h->tight;
     else if (!strcmp(key, "box")) *value = h->use_box;
+    else if (!strcmp(key, "reorder")) *value = h->reorder;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

@@ -39,6 +39,9 @@ struct FwdArgs {
     // update skips nodes outside `box`.  NULL: no box (every node is updated)
     int* box = nullptr;
     int* box_next = nullptr;
+    // processing order of the liquid particles (thread slot q works on particle
+    // order[q], a permutation inside each scene's liquid range) or NULL
+    const int* order = nullptr;
 };
 
 struct AdjArgs {
@@ -70,6 +73,7 @@ struct AdjArgs {
     const float4* vo2 = nullptr;     // grid velocity of substep f-1
     float* adj_prev = nullptr;       // adjoint slot of state f-1 (receives its position-adjoint part)
     const int* box = nullptr;        // occupied node box of substep f (see FwdArgs::box) or NULL
+    const int* order = nullptr;      // processing order (see FwdArgs::order) or NULL
 };
 
 // Counting sort of the particles of one substep by stencil-base cell.
@@ -161,6 +165,11 @@ struct ResortArgs {
     int* perm_out;           // [N] caller index of each new position
 };
 void launch_resort(const ResortArgs& r, int n_blocks, int block, int max_n, int n_scenes, cudaStream_t st);
+// The same interleaved order as a processing order only: r.dest receives the
+// new slot of each particle and order[slot] the particle; the state is not
+// moved (r.out, r.perm_in and r.perm_out are unused).
+void launch_order(const ResortArgs& r, int* order, int n_blocks, int block, int max_n, int n_scenes,
+                  cudaStream_t st);
 // out[c][p] = in[c][dest[p]]: the adjoint of the re-sort (adjoint in the new
 // order -> adjoint in the order before)
 void launch_unpermute(const float* in, float* out, const int* dest, long long stride, long long n,

@@ -39,6 +39,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
     long long p = bi.start + threadIdx.x;
     bool active = p < bi.end;
     if (!active) p = bi.end - 1;  // the lane computes a copy and writes nothing
+    if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
     float x[3], v[3], C[9];
     load3(a.cur, a.stride, OX, p, x);
     load3(a.cur, a.stride, OV, p, v);
@@ -197,6 +198,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
     bool active = p < bi.end;
     float dv[3] = {0.f, 0.f, 0.f};
     if (active) {
+        if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
         float x[3];
         load3(a.cur, a.stride, OX, p, x);
         int base[3];
@@ -459,6 +461,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
     bool active = p < bi.end;
     if (!WARP && !active) return;
     if (!active) p = bi.end - 1;  // WARP: the lane computes a copy and scatters nothing
+    if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
     float x[3];
     load3(a.cur, a.stride, OX, p, x);
     float xb[3] = {0.f, 0.f, 0.f}, vnb[3], Cb[9];
@@ -639,6 +642,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
     float pg[4] = {0.f, 0.f, 0.f, 0.f};
     if (p < bi.end) {
         const bool liquid = bi.kind == KIND_LIQUID;
+        if (a.order && liquid) p = a.order[p];
         float x[3];
         load3(a.cur, a.stride, OX, p, x);
         float m, mv[3], A[9];

@@ -69,10 +69,11 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 3, 'brick_scatter': 0}, {'p2g': 3, 'brick_scatter': 2}, {'p2g': 3, 'brick_gather': 0},
             {'p2g': 3, 'graph': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 4, 'resort': 0},
             {'p2g': 4, 'graph': 1}, {'p2g': 4, 'tight': 0}, {'p2g': 4, 'tight': 2},
-            {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'tight': 0}]
+            {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'tight': 0}, {'p2g': 4, 'reorder': 3},
+            {'p2g': 1, 'reorder': 2, 'graph': 1}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
-               'warp-tight0', 'warp-tight2', 'warp-fused-tight0']
+               'warp-tight0', 'warp-tight2', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
@@ -205,6 +206,36 @@ def test_box_skip_matches_full_grid(opts):
         assert rel(ds1[k], ds0[k]) < 1e-3, k
     assert rel(dp1, dp0) < 1e-4
     assert rel(fs1, fs0) < 1e-4
+
+
+@pytest.mark.parametrize('opts', [{'p2g': 4}, {'p2g': 1}, {'p2g': 4, 'graph': 1}, {'p2g': 4, 'resort': 0}],
+                         ids=['warp', 'vec', 'warp-graph', 'warp-noresort'])
+def test_processing_order_matches_fixed_order(opts):
+    """Rebuilding the processing order every 3 substeps inside 12-substep
+    segments changes only the order of the float atomics; recorded rollout,
+    reverse pass and an unrecorded rollout, two scenes."""
+    T, K = 36, 12
+    scenes = [rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=10)),
+              rounded(S.small_synthetic_scene(n_grid=20, ppc=4, n_steps=T, seed=11))]
+    wts = torch.as_tensor(np.random.default_rng(6).normal(size=(2, T, 3)), dtype=torch.float32, device='cuda')
+    out = {}
+    for ro in (0, 3):
+        sim = Simulator(scenes, max_steps=T, options=dict(opts, reorder=ro))
+        f = sim.forward(T, ckpt_every=K, record=True).cpu().numpy()
+        dp, ds = sim.backward(wts, want_state0=True)
+        sim.reset()
+        sim.forward(T, ckpt_every=K)
+        st = {k: v.cpu().numpy() for k, v in sim.get_state().items()}
+        assert sim.status() == 0
+        out[ro] = (f, st, dp.cpu().numpy(), {k: v.cpu().numpy() for k, v in ds.items()})
+        sim.close()
+    f0, st0, dp0, ds0 = out[0]
+    f1, st1, dp1, ds1 = out[3]
+    assert rel(f1, f0) < 1e-5
+    for k in 'xvCF':
+        assert rel(st1[k], st0[k]) < 1e-4, k
+        assert rel(ds1[k], ds0[k]) < 1e-3, k
+    assert rel(dp1, dp0) < 1e-4
 
 
 def test_checkpoint_interval_invariance():
