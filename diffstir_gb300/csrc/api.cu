@@ -163,7 +163,7 @@ struct DstirHandle {
     int resort = 1;             // option "resort": 0 never
     int tight = 1;              // option "tight": register-cap level of the particle kernels (0, 1, 2)
     int use_box = 1;            // option "box": the grid kernels skip nodes outside the occupied box
-    int reorder = 10;           // option "reorder": processing order rebuilt every this many substeps (0: never)
+    int reorder = 0;            // option "reorder": processing order rebuilt every this many substeps (0: never)
     int* vord = nullptr;        // [vord_slots][stride] processing orders (slot j: substeps [jR, (j+1)R) of a segment)
     long long vord_slots = 0;
     int* rs_vdest = nullptr;    // [stride] scratch of the processing-order build

@@ -154,7 +154,10 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * still cross the ABI in the order given to dstir_set_state), "tight" [1]
  * (register-cap level of the particle kernels, 0..2), "box" [1] (P2G records
  * each scene's occupied node box and the grid update and its adjoint skip the
- * nodes outside it; per-particle variants only), "brick_scatter" /
+ * nodes outside it; per-particle variants only), "reorder" [0] (rebuild the
+ * interleaved order every this many substeps as a processing order only: the
+ * kernels read the state through an index; measured slower than the physical
+ * re-sort alone at 64^3), "brick_scatter" /
  * "brick_gather" (scatter and gather forms of variant 3), "profile" [0] (1:
  * time every launch with CUDA events; totals via dstir_get_option
  * "prof_ns:<kernel>" / "prof_count:<kernel>"), "launches" (reset the launch
