@@ -268,8 +268,7 @@ def run_ours(args):
     ys = S_yield(args.config)
 
     # target force profiles from seeded ground-truth parameters
-    nr = S.config_n_range(args.config)
-    true_p = torch.tensor(np.stack([S.draw_params(rng, ys, nr) for _ in range(B)]), dtype=torch.float32,
+    true_p = torch.tensor(np.stack([S.draw_config_params(args.config, rng) for _ in range(B)]), dtype=torch.float32,
                           device=dev)
     sim.set_params(true_p)
     sim.reset()

@@ -674,10 +674,20 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
                    int box0, cudaStream_t st) {
     // box0: occupied-box slot of substep 0 of this chain
     reset_boxes(h, box0, nsteps, st);
+    // Without clear_pm every substep scatters into its own P2G grid slot (the
+    // segment recompute, whose grids the reverse pass reads); the slot is
+    // zeroed right before its scatter so that the zeroed lines are still in L2
+    auto zero_slot = [&](int k) {
+        if (clear_pm) return;
+        float4 *pm, *vo;
+        grids(k, pm, vo);
+        cudaMemsetAsync(pm, 0, (size_t)h->G * sizeof(float4), st);
+    };
     if (!fused(h)) {
         for (int k = 0; k < nsteps; ++k) {
             float4 *pm, *vo;
             grids(k, pm, vo);
+            zero_slot(k);
             FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + k, force, fstride, fo0 + k, clear_pm);
             a.box = box_slot(h, box0 + k);
             // per_step_bins marks the segment recompute, whose orders the
@@ -691,6 +701,7 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
     {
         float4 *pm, *vo;
         grids(0, pm, vo);
+        zero_slot(0);
         FwdArgs a = fwd_args(h, slot(0), slot(1), pm, vo, t0, force, fstride, fo0, clear_pm);
         a.box = box_slot(h, box0);
         timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st, h->tight); });
@@ -704,6 +715,7 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
         if (k + 1 < nsteps) {
             float4 *pmn, *von;
             grids(k + 1, pmn, von);
+            zero_slot(k + 1);
             a.next2 = slot(k + 2);
             a.pm_next = pmn;
             a.box_next = box_slot(h, box0 + k + 1);
@@ -1002,7 +1014,6 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
         int L = std::min(K, n - s0);
         float* slot0 = h->ckpt + (size_t)sgi * sf;
         auto slot = [&](int j) -> float* { return j == 0 ? slot0 : h->seg + (size_t)(j - 1) * sf; };
-        cudaMemsetAsync(h->pm, 0, (size_t)L * h->G * sizeof(float4), st);
         auto grids = [&](int k, float4*& pm, float4*& vo) {
             pm = h->pm + (size_t)k * h->G;
             vo = h->vo + (size_t)k * h->G;

@@ -243,7 +243,7 @@ def main(argv=None):
     T = args.substeps or cfg['n_steps']
     R = args.restarts or cfg.get('restarts', 16)
     rng = np.random.default_rng(args.seed)
-    truth = S.draw_params(rng, cfg.get('yield_stress', False), cfg.get('n_range', (0.4, 1.2)))
+    truth = S.draw_config_params(args.config, rng)
     sc = S.synthetic_scene(args.config, seed=args.seed, n_steps=T, params=truth)
     sim = Simulator(sc, max_steps=T)
     clean = sim.forward(T)[0].cpu().numpy()

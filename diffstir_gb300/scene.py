@@ -342,9 +342,14 @@ CONFIGS = {
     'C3': dict(n_grid=64, ppc=8, lo=(0.2, 0.05, 0.2), hi=(0.8, None, 0.8), dt=2e-4, n_steps=1000,
                params=None, rod_radius=0.03, path='circle', ckpt=50, batch=64, yield_stress=True,
                n_range=(0.4, 0.85)),
-    # 128^3, 8 ppc, ~4.8M particles, 4000 substeps, r=0.02, sinusoid path
+    # 128^3, 8 ppc, ~4.8M particles, 4000 substeps, r=0.02, sinusoid path.
+    # Fixed power law K=0.3, n=0.7: at dx=1/128 the explicit viscous limit of
+    # dt=2e-4 is four times tighter than at 64^3, and draws such as K=1.57,
+    # n=0.91 or K=0.5, n=0.9 blow up within a few hundred substeps, while
+    # K=0.3, n=0.7 (and K<=2 with n<=0.5) stay stable over 1000 substeps.
     'C4': dict(n_grid=128, ppc=8, lo=(0.1, 0.05, 0.1), hi=(0.9, 0.5, 0.9), dt=2e-4, n_steps=4000,
-               params=None, rod_radius=0.02, path='sinusoids', ckpt=100),
+               params=(0.3, 0.0, 0.7, 0.0), rod_radius=0.02, path='sinusoids', ckpt=100,
+               k_range=(0.1, 0.5), n_range=(0.5, 0.7)),
     # 64^3, ~410k particles, 1500 substeps, identification with 16 restarts
     'C5': dict(n_grid=64, ppc=8, lo=(0.15, 0.05, 0.15), hi=(0.85, 0.45, 0.85), dt=2e-4,
                n_steps=1500, params=None, rod_radius=0.03, path='circle', ckpt=50, restarts=16,
@@ -352,11 +357,11 @@ CONFIGS = {
 }
 
 
-def draw_params(rng, yield_stress=False, n_range=(0.4, 1.2)):
-    """(K, tau_y, n) of the synthetic workloads: K ~ U[0.1, 2], n ~ U[n_range],
+def draw_params(rng, yield_stress=False, n_range=(0.4, 1.2), k_range=(0.1, 2.0)):
+    """(K, tau_y, n) of the synthetic workloads: K ~ U[k_range], n ~ U[n_range],
     tau_y ~ U[0, 5] (or 0).  Returned in the reference's parameter order
     [K, tau_y, n, unused] (simulation_functions.py:138-146)."""
-    K = rng.uniform(0.1, 2.0)
+    K = rng.uniform(*k_range)
     n = rng.uniform(*n_range)
     tau = rng.uniform(0.0, 5.0) if yield_stress else 0.0
     return np.array([K, tau, n, 0.0])
@@ -364,6 +369,16 @@ def draw_params(rng, yield_stress=False, n_range=(0.4, 1.2)):
 
 def config_n_range(name):
     return CONFIGS[name].get('n_range', (0.4, 1.2))
+
+
+def config_k_range(name):
+    return CONFIGS[name].get('k_range', (0.1, 2.0))
+
+
+def draw_config_params(name, rng):
+    """Seeded ground-truth parameters for configuration ``name``."""
+    cfg = CONFIGS[name]
+    return draw_params(rng, cfg.get('yield_stress', False), config_n_range(name), config_k_range(name))
 
 
 def synthetic_scene(name='C1', seed=0, n_steps=None, n_grid=None, fill_height=None, params=None,
@@ -379,8 +394,7 @@ def synthetic_scene(name='C1', seed=0, n_steps=None, n_grid=None, fill_height=No
         hi[1] = fill_height if fill_height is not None else rng.uniform(0.15, 0.45)
     pos = block_particles(ng, cfg['ppc'], lo, hi, rng)
     if params is None:
-        params = cfg['params'] if cfg['params'] is not None else draw_params(
-            rng, cfg.get('yield_stress', False), cfg.get('n_range', (0.4, 1.2)))
+        params = cfg['params'] if cfg['params'] is not None else draw_config_params(name, rng)
     if cfg['path'] == 'circle':
         traj = circle_trajectory(T, cfg['dt'])
     else:
