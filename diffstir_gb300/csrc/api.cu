@@ -24,11 +24,13 @@ using namespace dstir;
 
 namespace {
 // kernel kinds timed by the optional in-library profiler
+// (the *_rc kinds are the same kernels inside the reverse pass's segment
+// recompute; "p2g" etc. count the forward rollouts only)
 enum { K_P2G = 0, K_GRID, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_BIN, K_G2P_P2G, K_P2G_ADJ_G2P_ADJ, K_OTHER,
-       K_NUM };
-const char* const kKernelNames[K_NUM] = {"p2g",     "grid",    "g2p",                "g2p_adj", "grid_adj",
-                                         "p2g_adj", "bin",     "g2p_p2g",            "p2g_adj_g2p_adj",
-                                         "other"};
+       K_P2G_RC, K_GRID_RC, K_G2P_RC, K_BIN_RC, K_G2P_P2G_RC, K_NUM };
+const char* const kKernelNames[K_NUM] = {"p2g",     "grid",     "g2p",    "g2p_adj", "grid_adj",
+                                         "p2g_adj", "bin",      "g2p_p2g", "p2g_adj_g2p_adj",
+                                         "other",   "p2g_rc",   "grid_rc", "g2p_rc", "bin_rc", "g2p_p2g_rc"};
 
 // CUDA-event timing of every launch on the launching stream.  Event pairs live
 // in a ring; a pair is read back (synchronising on its stop event) when the
@@ -199,6 +201,7 @@ struct DstirHandle {
     long long fwd_key[8] = {0}, bwd_key[8] = {0};
 
     int cur = 0;  // work slot holding the current state
+    bool in_recompute = false;  // profiler: launches belong to a segment recompute
     bool recorded = false;
     int rec_t0 = 0, rec_n = 0, rec_K = 0;
     std::string err;
@@ -340,6 +343,13 @@ void timed(DstirHandle* h, int kind, cudaStream_t st, Fn fn) {
     if (!h->prof.on || h->capturing) {
         fn();
         return;
+    }
+    if (h->in_recompute) {
+        if (kind == K_P2G) kind = K_P2G_RC;
+        else if (kind == K_GRID) kind = K_GRID_RC;
+        else if (kind == K_G2P) kind = K_G2P_RC;
+        else if (kind == K_BIN) kind = K_BIN_RC;
+        else if (kind == K_G2P_P2G) kind = K_G2P_P2G_RC;
     }
     size_t i = h->prof.begin(kind, st);
     fn();
@@ -1020,8 +1030,10 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
         };
         // recompute the segment, keeping every state and grid; the state after
         // its last substep is not needed by the adjoint
+        h->in_recompute = true;
         chain_forward(h, t0 + s0, L, slot, grids, h->force_scratch, (long long)h->max_steps * 3, t0 + s0, 0, true,
                       true, s0, st);
+        h->in_recompute = false;
         // adjoint of the state at global step g (relative to t0) lives in A[(n - g) & 1]
         auto adj_args = [&](int k) {
             AdjArgs a;
