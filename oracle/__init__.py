@@ -6,7 +6,12 @@ stand-in for the reference; the diffstir_gb300 product never does.
 
 ``build()`` compiles oracle.cpp (a line-by-line C++ restatement of
 src/simulator/simulation_functions.py with a hand-derived adjoint) into
-``oracle/_build/liboracle.so`` with g++ and OpenMP.
+``oracle/_build/liboracle.so`` with g++ and OpenMP.  The diagnostic variant
+``continuous_top`` (``liboracle_continuous_top.so``) replaces the reference's
+sticky top (a node of the top band loses its whole velocity when v_y > 0,
+simulation_functions.py:221-224) by a clamp of v_y alone; it exists only to
+show that this discontinuous rule is what separates adjoint and difference
+quotients once the fluid reaches the top band.
 """
 
 import ctypes as C
@@ -19,29 +24,31 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, 'oracle.cpp')
 OUT_DIR = os.path.join(HERE, '_build')
 LIB = os.path.join(OUT_DIR, 'liboracle.so')
+VARIANTS = {None: ([], 'liboracle.so'),
+            'continuous_top': (['-DORACLE_CONTINUOUS_TOP'], 'liboracle_continuous_top.so')}
 
-_lib = None
+_libs = {}
 
 
-def build(force=False):
+def build(force=False, variant=None):
     os.makedirs(OUT_DIR, exist_ok=True)
+    flags, name = VARIANTS[variant]
+    lib = os.path.join(OUT_DIR, name)
     hdr = os.path.join(HERE, '..', 'include', 'diffstir.h')
-    if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr))):
-        return LIB
-    tmp = LIB + '.tmp%d' % os.getpid()
-    cmd = ['g++', '-O2', '-std=c++17', '-fopenmp', '-fPIC', '-shared', '-o', tmp, SRC]
+    if (not force and os.path.exists(lib)
+            and os.path.getmtime(lib) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr))):
+        return lib
+    tmp = lib + '.tmp%d' % os.getpid()
+    cmd = ['g++', '-O2', '-std=c++17', '-fopenmp', '-fPIC', '-shared'] + flags + ['-o', tmp, SRC]
     subprocess.run(cmd, check=True)
-    os.replace(tmp, LIB)
-    return LIB
+    os.replace(tmp, lib)
+    return lib
 
 
-def load():
-    global _lib
-    if _lib is None:
+def load(variant=None):
+    if variant not in _libs:
         from diffstir_gb300._abi import DstirSceneDesc
-        build()
-        lib = C.CDLL(LIB)
+        lib = C.CDLL(build(variant=variant))
         D = C.POINTER(C.c_double)
         sig_roll = [C.POINTER(DstirSceneDesc), D, D, C.c_int, D, D, D, D, D, D, C.c_int]
         sig_grad = [C.POINTER(DstirSceneDesc), D, D, C.c_int, D, D, D, D, D, D, D, D, C.c_int]
@@ -59,8 +66,8 @@ def load():
         lib.oracle_svd3_backward_f64.argtypes = [D, D, D, D, D, D, D, C.c_int64]
         lib.oracle_svd3_backward_f64.restype = None
         lib.oracle_max_threads.restype = C.c_int
-        _lib = lib
-    return _lib
+        _libs[variant] = lib
+    return _libs[variant]
 
 
 def _p(a):
@@ -79,9 +86,9 @@ def _arr(a, shape=None):
 
 
 def rollout(desc, params, traj, T, x0, v0=None, C0=None, F0=None, precision='f64',
-            threads=1, return_states=False):
+            threads=1, return_states=False, variant=None):
     """Forward rollout; returns (force [T,3], states [(T+1),N,24] or None, status)."""
-    lib = load()
+    lib = load(variant)
     N = desc.n_liquid + desc.n_rod + desc.n_container
     params, traj = _arr(params), _arr(traj)
     x0, v0, C0, F0 = _arr(x0), _arr(v0), _arr(C0), _arr(F0)
@@ -96,9 +103,9 @@ def rollout(desc, params, traj, T, x0, v0=None, C0=None, F0=None, precision='f64
 
 
 def grad(desc, params, traj, T, x0, dL_dforce, v0=None, C0=None, F0=None, precision='f64',
-         threads=1, want_state0=False):
+         threads=1, want_state0=False, variant=None):
     """Rollout + reverse pass; returns (force, dL_dparams[4], dL_dstate0 [N,24] or None, status)."""
-    lib = load()
+    lib = load(variant)
     N = desc.n_liquid + desc.n_rod + desc.n_container
     params, traj = _arr(params), _arr(traj)
     x0, v0, C0, F0 = _arr(x0), _arr(v0), _arr(C0), _arr(F0)

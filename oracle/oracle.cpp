@@ -459,7 +459,12 @@ struct Sim {
             if (k < b && v[2] < 0) v[2] = 0;
             if (k > n - b && v[2] > 0) v[2] = 0;
             if (j < b && v[1] < 0) v[1] = 0;
-            if (j > n - b && v[1] > 0) { v[0] = 0; v[1] = 0; v[2] = 0; }
+#ifdef ORACLE_CONTINUOUS_TOP
+            // diagnostic build: a plain clamp instead of the sticky top
+            if (j > n - b && v[1] > 0) v[1] = 0;
+#else
+            if (j > n - b && v[1] > 0) { v[0] = 0; v[1] = 0; v[2] = 0; }  // sticky top, :221-224
+#endif
             if (cyl) {
                 R ddx = R(i) * dx - rc[0], ddz = R(k) * dx - rc[2];
                 R rr = R(d.rod_radius);
@@ -736,7 +741,11 @@ struct Sim {
             if (k < b && v[2] < 0) { v[2] = 0; mask[2] = 0; }
             if (k > n - b && v[2] > 0) { v[2] = 0; mask[2] = 0; }
             if (j < b && v[1] < 0) { v[1] = 0; mask[1] = 0; }
+#ifdef ORACLE_CONTINUOUS_TOP
+            if (j > n - b && v[1] > 0) { v[1] = 0; mask[1] = 0; }
+#else
             if (j > n - b && v[1] > 0) { mask[0] = mask[1] = mask[2] = 0; }
+#endif
             R ub[3];
             R mb = 0;
             bool inside = false;

@@ -3,6 +3,8 @@ restated equations), on the parts of the path the reference scene does not
 exercise: the moving-cylinder rod, the SVD-determinant mode, the three models
 with the MSE force loss of the synthetic scenes, and the SVD kernels."""
 
+import os
+
 import numpy as np
 import pytest
 
@@ -148,3 +150,48 @@ def test_segment_chaining_equals_one_shot():
         dp += d
     np.testing.assert_allclose(dp, dp1, rtol=1e-12, atol=1e-14)
     np.testing.assert_allclose(adj, ds1, rtol=1e-12, atol=1e-14)
+
+
+@pytest.mark.skipif(not os.environ.get('DIFFSTIR_SLOW'), reason='several minutes of CPU; set DIFFSTIR_SLOW=1')
+def test_sticky_top_is_what_separates_adjoint_and_differences():
+    """The 64^3 workload's block and parameters at 32^3 over 1000 substeps: the
+    fluid reaches the top band (j > n - bound) after ~300 substeps.  With the
+    reference's sticky top (a top-band node loses its whole velocity when
+    v_y > 0, simulation_functions.py:221-224) the loss has many small jumps in
+    the parameters, so central differences (h = 1e-4 x |param|) move away from
+    the adjoint; with that rule replaced by a plain clamp of v_y the two agree
+    to 1e-5 again.  FP64 throughout."""
+    cfg = S.CONFIGS['C2']
+    p = np.array([0.11404720693826675, 0.0, 0.8690828084945679, 0.0])
+    truth = S.draw_config_params('C2', np.random.default_rng(1000))
+    pos = S.block_particles(32, 8, cfg['lo'], cfg['hi'], np.random.default_rng(0))
+    desc = S.synthetic_desc(32, 8, pos.shape[0], dt=cfg['dt'], rod_radius=cfg['rod_radius'])
+    T = 1000
+    traj = S.circle_trajectory(T, cfg['dt'])
+    thr = oracle.max_threads()
+    gaps = {}
+    for variant in (None, 'continuous_top'):
+        ft, _, st = oracle.rollout(desc, truth, traj, T, pos, threads=thr, variant=variant)
+        assert st == 0
+
+        def loss(pp):
+            f, _, s = oracle.rollout(desc, pp, traj, T, pos, threads=thr, variant=variant)
+            d = (f - ft)[:, 0::2]
+            return (d * d).sum() / d.size, f
+
+        _, f0 = loss(p)
+        d = (f0 - ft)[:, 0::2]
+        w = np.zeros((T, 3))
+        w[:, 0::2] = 2 * d / d.size
+        _, dp, _, _ = oracle.grad(desc, p, traj, T, pos, w, threads=thr, variant=variant)
+        rel = []
+        for i in (0, 2):
+            h = 1e-4 * abs(p[i])
+            pp, pm = p.copy(), p.copy()
+            pp[i] += h
+            pm[i] -= h
+            fd = (loss(pp)[0] - loss(pm)[0]) / (2 * h)
+            rel.append(abs(fd - dp[i]) / abs(fd))
+        gaps[variant] = max(rel)
+    assert gaps[None] > 1e-3
+    assert gaps['continuous_top'] < 1e-5
