@@ -385,6 +385,36 @@ def run_ours(args):
                               '(simulation_functions.py:221-224) makes the loss jump in the parameters and the '
                               'quotients drift from the pointwise derivative by ~1e-3 even in FP64; the adjoint '
                               'is checked against the FP64 oracle adjoint instead (tests)'}
+        # the same check over the first substeps only, before the fluid can
+        # reach the top band (the 64^3 scene first touches it after ~525)
+        Ts = min(T, 400)
+        if Ts < T:
+            fs_t = target[:, :Ts]
+
+            def short_losses(p):
+                sim.set_params(p)
+                sim.reset()
+                f = sim.forward(Ts)
+                diff = (f - fs_t)[..., 0::2].double()
+                return (diff * diff).sum(dim=(1, 2)) / float(B * Ts * 2)
+
+            sim.set_params(params)
+            sim.reset()
+            f = sim.forward(Ts, ckpt_every=ckpt, record=True)
+            diff = (f - fs_t)[..., 0::2]
+            dF = torch.zeros_like(f)
+            dF[..., 0::2] = 2.0 * diff / float(B * Ts * 2)
+            dp_s = sim.backward(dF)
+            errs = {}
+            for i in free:
+                hs = args.fd_h * params[:, i].abs().clamp_min(1e-3)
+                pp, pm = params.clone(), params.clone()
+                pp[:, i] += hs
+                pm[:, i] -= hs
+                fd = (short_losses(pp) - short_losses(pm)) / (2.0 * hs.double())
+                errs[names[i]] = float(((dp_s[:, i].double() - fd).abs() / fd.abs().clamp_min(1e-30)).max())
+            grad_check['first_%d_substeps' % Ts] = {'h_rel': args.fd_h, 'rel_err': errs,
+                                                    'rel_err_max': max(errs.values())}
         for hr in sorted({args.fd_h, 1e-2}):
             errs, nse = {}, {}
             for i in free:
