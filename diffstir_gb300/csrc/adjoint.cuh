@@ -67,6 +67,77 @@ __device__ __forceinline__ void p2g_adj_node(float W, float dWx, float dWy, floa
     }
 }
 
+// The same 27-node gather in factored form.  With dp = (o - fx) dx for node
+// offset o = (i, j, k):
+//   A dp + m v'         = c + dx (i A_0 + j A_1 + k A_2),   c = m v' - dx A fx
+//   Ab = sum W g dp^T   = dx (T - S fx^T),  S = sum W g,  T = sum W g o^T
+//   fxb -= dx sum W A^T g  ->  -dx A^T S, once after the loop,
+// so a node costs its weight products, one float4 load, a 4-term dot product
+// for Wb and a handful of adds, instead of the three 3x3 products of
+// p2g_adj_node.  `pmb` is the P/M-adjoint grid, `row0` the node index of the
+// stencil base (k innermost).
+__device__ __forceinline__ void p2g_adj_gather(const float4* __restrict__ pmb, const SceneDev& s,
+                                               const int base[3], const float fx[3], const float w[3][3],
+                                               const float dw[3][3], float m, const float mv[3],
+                                               const float A[9], bool liquid, float Ab[9], float vvb[3],
+                                               float fxb[3]) {
+    const float dx = s.dx;
+    float c[3], Ad[9];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        c[a] = mv[a] - dx * (A[a * 3 + 0] * fx[0] + A[a * 3 + 1] * fx[1] + A[a * 3 + 2] * fx[2]);
+#pragma unroll
+        for (int b = 0; b < 3; ++b) Ad[a * 3 + b] = dx * A[a * 3 + b];
+    }
+    float S[3] = {0.f, 0.f, 0.f}, T[9];
+#pragma unroll
+    for (int q = 0; q < 9; ++q) T[q] = 0.f;
+    float fb[3] = {0.f, 0.f, 0.f};
+#pragma unroll
+    for (int i = 0; i < 3; ++i)
+#pragma unroll
+        for (int j = 0; j < 3; ++j) {
+            const float4* rowp = pmb + node_index(s, base[0] + i, base[1] + j, base[2]);
+            const float wij = w[i][0] * w[j][1], dxij = dw[i][0] * w[j][1], dyij = w[i][0] * dw[j][1];
+            float r[3];
+#pragma unroll
+            for (int a = 0; a < 3; ++a) r[a] = c[a] + (float)i * Ad[a * 3 + 0] + (float)j * Ad[a * 3 + 1];
+#pragma unroll
+            for (int k = 0; k < 3; ++k) {
+                const float4 g = __ldg(rowp + k);
+                const float W = wij * w[k][2];
+                const float rk0 = r[0] + (float)k * Ad[2], rk1 = r[1] + (float)k * Ad[5], rk2 = r[2] + (float)k * Ad[8];
+                const float Wb = g.w * m + g.x * rk0 + g.y * rk1 + g.z * rk2;
+                const float wg[3] = {W * g.x, W * g.y, W * g.z};
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    S[a] += wg[a];
+                    if (i) T[a * 3 + 0] += (float)i * wg[a];
+                    if (j) T[a * 3 + 1] += (float)j * wg[a];
+                    if (k) T[a * 3 + 2] += (float)k * wg[a];
+                }
+                if (liquid) {
+                    fb[0] += Wb * dxij * w[k][2];
+                    fb[1] += Wb * dyij * w[k][2];
+                    fb[2] += Wb * wij * dw[k][2];
+                }
+            }
+        }
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        vvb[a] = S[a];
+#pragma unroll
+        for (int b = 0; b < 3; ++b) Ab[a * 3 + b] = dx * (T[a * 3 + b] - fx[b] * S[a]);
+    }
+    if (liquid) {
+#pragma unroll
+        for (int b = 0; b < 3; ++b)
+            fxb[b] = fb[b] - (Ad[0 * 3 + b] * S[0] + Ad[1 * 3 + b] * S[1] + Ad[2 * 3 + b] * S[2]);
+    } else {
+        fxb[0] = fxb[1] = fxb[2] = 0.f;
+    }
+}
+
 // The adjoint of the state at substep f (xb, vb, Cb, Fb) from the stencil
 // gather results; parameter partials are added to pg.
 template <bool SVDJ>
