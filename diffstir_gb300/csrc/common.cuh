@@ -47,6 +47,26 @@ struct GridBlock {
     long long start, end;
 };
 
+// (i, j, k) of a scene-local node index (k innermost) in 32-bit arithmetic;
+// n <= 1024, so local < 2^30
+__device__ __forceinline__ void node_ijk(int local, int n, int& i, int& j, int& k) {
+    const int nn = n * n;
+    i = local / nn;
+    const int r = local - i * nn;
+    j = r / n;
+    k = r - j * n;
+}
+
+// Block-cooperative copy of a scene descriptor into shared memory (one word
+// per thread of the first warp instead of a serial struct copy by thread 0).
+// Call from every thread of the block; a __syncthreads() must follow.
+__device__ __forceinline__ void load_scene_shared(SceneDev& dst, const SceneDev* src) {
+    static_assert(sizeof(SceneDev) % 4 == 0 && sizeof(SceneDev) / 4 <= 32, "SceneDev copy");
+    const int words = (int)(sizeof(SceneDev) / 4);
+    if (threadIdx.x < words)
+        reinterpret_cast<int*>(&dst)[threadIdx.x] = __ldg(reinterpret_cast<const int*>(src) + threadIdx.x);
+}
+
 __device__ __forceinline__ float* comp(float* st, long long stride, int c) { return st + (long long)c * stride; }
 __device__ __forceinline__ const float* comp(const float* st, long long stride, int c) {
     return st + (long long)c * stride;

@@ -128,24 +128,23 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
 
 __global__ void __launch_bounds__(256) grid_kernel(FwdArgs a) {
     __shared__ SceneDev s;
-    __shared__ GridBlock gb;
     __shared__ float sh[32][4];
-    __shared__ float rc[3], rodv[3];
-    if (threadIdx.x == 0) {
-        gb = a.gblk[blockIdx.x];
-        s = a.sc[gb.scene];
+    __shared__ float rc[3], rc1[3];
+    // every thread reads the block descriptor (one broadcast load), so the
+    // scene copy and the trajectory loads do not wait on a serial chain
+    const GridBlock gb = a.gblk[blockIdx.x];
+    load_scene_shared(s, a.sc + gb.scene);
+    if (threadIdx.x < 3) {
         const float* t0 = a.traj + ((long long)gb.scene * a.traj_len + a.f) * 3;
-        for (int c = 0; c < 3; ++c) {
-            rc[c] = t0[c];
-            rodv[c] = (t0[3 + c] - t0[c]) / s.dt;
-        }
+        rc[threadIdx.x] = t0[threadIdx.x];
+        rc1[threadIdx.x] = t0[3 + threadIdx.x];
     }
     __syncthreads();
     long long node = gb.start + threadIdx.x;
     float fsum[3] = {0.f, 0.f, 0.f};
-    const long long local = node - s.goff;
     const int n = s.n;
-    const int i = (int)(local / ((long long)n * n)), j = (int)((local / n) % n), k = (int)(local % n);
+    int i, j, k;
+    node_ijk((int)(node - s.goff), n, i, j, k);
     // nodes outside the occupied box hold no mass and no stencil reads them:
     // their P2G entry is still zero and their velocity is never gathered
     if (node < gb.end && (!a.box || box_inside(a.box + gb.scene * 6, i, j, k))) {
@@ -176,9 +175,10 @@ __global__ void __launch_bounds__(256) grid_kernel(FwdArgs a) {
             if (ex * ex + ez * ez < s.rod_r2 && (float)j * s.dx >= rc[1]) {
 #pragma unroll
                 for (int c = 0; c < 3; ++c) {
+                    const float rodv = (rc1[c] - rc[c]) / s.dt;
                     float u = inv_m * (c == 0 ? g.x : (c == 1 ? g.y : g.z));
-                    fsum[c] = g.w * (rodv[c] - u) / s.dt;
-                    v[c] = rodv[c];
+                    fsum[c] = g.w * (rodv - u) / s.dt;
+                    v[c] = rodv;
                 }
             }
         }
@@ -568,25 +568,24 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
 
 __global__ void __launch_bounds__(256) grid_adj_kernel(AdjArgs a) {
     __shared__ SceneDev s;
-    __shared__ GridBlock gb;
     __shared__ float rc[3], rodv[3], fb[3];
-    if (threadIdx.x == 0) {
-        gb = a.gblk[blockIdx.x];
-        s = a.sc[gb.scene];
+    const GridBlock gb = a.gblk[blockIdx.x];
+    load_scene_shared(s, a.sc + gb.scene);
+    __syncthreads();
+    if (threadIdx.x < 3) {
+        const int c = threadIdx.x;
         const float* t0 = a.traj + ((long long)gb.scene * a.traj_len + a.f) * 3;
         const float* d = a.dforce + gb.scene * a.dforce_stride + (long long)a.fo * 3;
-        for (int c = 0; c < 3; ++c) {
-            rc[c] = t0[c];
-            rodv[c] = (t0[3 + c] - t0[c]) / s.dt;
-            fb[c] = d[c];
-        }
+        rc[c] = t0[c];
+        rodv[c] = (t0[3 + c] - t0[c]) / s.dt;
+        fb[c] = d[c];
     }
     __syncthreads();
     long long node = gb.start + threadIdx.x;
     if (node >= gb.end) return;
-    long long local = node - s.goff;
-    int n = s.n;
-    int i = (int)(local / ((long long)n * n)), j = (int)((local / n) % n), k = (int)(local % n);
+    const int n = s.n;
+    int i, j, k;
+    node_ijk((int)(node - s.goff), n, i, j, k);
     // outside the occupied box the velocity adjoint is zero (no stencil
     // scattered there) and no stencil gathers the P/M adjoint
     if (a.box && !box_inside(a.box + gb.scene * 6, i, j, k)) return;
