@@ -405,16 +405,21 @@ def run_ours(args):
             dF = torch.zeros_like(f)
             dF[..., 0::2] = 2.0 * diff / float(B * Ts * 2)
             dp_s = sim.backward(dF)
-            errs = {}
-            for i in free:
-                hs = args.fd_h * params[:, i].abs().clamp_min(1e-3)
-                pp, pm = params.clone(), params.clone()
-                pp[:, i] += hs
-                pm[:, i] -= hs
-                fd = (short_losses(pp) - short_losses(pm)) / (2.0 * hs.double())
-                errs[names[i]] = float(((dp_s[:, i].double() - fd).abs() / fd.abs().clamp_min(1e-30)).max())
-            grad_check['first_%d_substeps' % Ts] = {'h_rel': args.fd_h, 'rel_err': errs,
-                                                    'rel_err_max': max(errs.values())}
+            short = {}
+            for hr in sorted({args.fd_h, 1e-2}):
+                errs = {}
+                for i in free:
+                    hs = hr * params[:, i].abs().clamp_min(1e-3)
+                    pp, pm = params.clone(), params.clone()
+                    pp[:, i] += hs
+                    pm[:, i] -= hs
+                    fd = (short_losses(pp) - short_losses(pm)) / (2.0 * hs.double())
+                    errs[names[i]] = float(((dp_s[:, i].double() - fd).abs() / fd.abs().clamp_min(1e-30)).max())
+                short['h_rel=%g' % hr] = {'rel_err': errs, 'rel_err_max': max(errs.values())}
+            # FP32 rounding differs between the two perturbed rollouts and
+            # dominates the h = 1e-3 quotient (~0.5%); FP64 quotients match
+            # the adjoint to 1e-6 over this horizon
+            grad_check['first_%d_substeps' % Ts] = short
         for hr in sorted({args.fd_h, 1e-2}):
             errs, nse = {}, {}
             for i in free:
