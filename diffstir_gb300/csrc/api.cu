@@ -166,6 +166,8 @@ struct DstirHandle {
     int tight = 1;              // option "tight": register-cap level of the particle kernels (0, 1, 2)
     int use_box = 1;            // option "box": the grid kernels skip nodes outside the occupied box
     int reorder = 0;            // option "reorder": processing order rebuilt every this many substeps (0: never)
+    int store_grids = 0;        // option "store_grids": a recorded rollout keeps every substep's grids
+    bool rec_store = false;     // the recorded rollout kept its grids
     int* vord = nullptr;        // [vord_slots][stride] processing orders (slot j: substeps [jR, (j+1)R) of a segment)
     long long vord_slots = 0;
     int* rs_vdest = nullptr;    // [stride] scratch of the processing-order build
@@ -853,25 +855,30 @@ int forward_final_slot(const DstirHandle* h, int nsteps, int K, bool record) {
 // end of every chunk but the last is re-sorted into the next chunk's start
 // slot; otherwise the chunks simply continue ((cur + k) % 3).  Returns the
 // work slot of the final state.
-int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, cudaStream_t st) {
+int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, bool store, cudaStream_t st) {
     size_t sf = slot_floats(h);
     float* W[3] = {h->work, h->work + sf, h->work + 2 * sf};
     const int cur = h->cur;
+    // store: substep k scatters into grid slot k and keeps it (and its
+    // velocity grid) for the reverse pass; otherwise one slot is reused
+    const int clear_pm = store ? 0 : 1;
     if (record) {
         cudaMemcpyAsync(h->ckpt, W[cur], sf * sizeof(float), cudaMemcpyDeviceToDevice, st);
         cudaMemcpyAsync(h->perm_rec0, h->perm_cur, (size_t)h->N * sizeof(int), cudaMemcpyDeviceToDevice, st);
     }
     cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st);
-    auto grids = [&](int, float4*& pm, float4*& vo) {
-        pm = h->pm;
-        vo = h->vo;
+    int gk0 = 0;  // substep of the current chain's first grid slot (store mode)
+    auto grids = [&](int k, float4*& pm, float4*& vo) {
+        pm = store ? h->pm + (size_t)(gk0 + k) * h->G : h->pm;
+        vo = store ? h->vo + (size_t)(gk0 + k) * h->G : h->vo;
     };
     if (!resort_count(h, nsteps, K)) {
         auto slot = [&](int k) -> float* {
             if (record && k % K == 0 && k < nsteps) return h->ckpt + (size_t)(k / K) * sf;
             return W[(cur + k) % 3];
         };
-        chain_forward(h, t0, nsteps, slot, grids, h->fbuf, (long long)h->max_steps * 3, 0, 1, false, false, 0, st);
+        chain_forward(h, t0, nsteps, slot, grids, h->fbuf, (long long)h->max_steps * 3, 0, clear_pm, false, false, 0,
+                      st);
         return (cur + nsteps) % 3;
     }
     int a = cur;
@@ -879,7 +886,9 @@ int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, cuda
     for (int c = 0, k0 = 0;; ++c) {
         const int L = std::min(K, nsteps - k0);
         auto slot = [&](int j) -> float* { return j == 0 ? in : W[(a + j) % 3]; };
-        chain_forward(h, t0 + k0, L, slot, grids, h->fbuf, (long long)h->max_steps * 3, k0, 1, false, false, k0, st);
+        gk0 = k0;
+        chain_forward(h, t0 + k0, L, slot, grids, h->fbuf, (long long)h->max_steps * 3, k0, clear_pm, false, false, k0,
+                      st);
         const int out = (a + L) % 3;
         if (k0 + L >= nsteps) return out;
         float* next = record ? h->ckpt + (size_t)(c + 1) * sf : W[(out + 1) % 3];
@@ -959,11 +968,14 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
     const long long nres = resort_count(h, nsteps, K);
     if (nres && (rc = ensure_resort(h, record ? nseg : 1))) return rc;
     if ((rc = ensure_vorder(h, K))) return rc;
+    const bool store = record && h->store_grids && !binned(h) && !fused(h);
+    if (store && (rc = ensure_grid_slots(h, nsteps))) return rc;
     long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch,
-                         h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0) + (vorder_on(h) ? 512 * h->reorder : 0),
+                         h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0) + (vorder_on(h) ? 512 * h->reorder : 0) +
+                             (store ? (1LL << 40) : 0),
                          h->block * 4096 + h->gblock};
     rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want,
-                         [&](cudaStream_t s2) { enqueue_forward(h, t0, nsteps, K, record != 0, s2); });
+                         [&](cudaStream_t s2) { enqueue_forward(h, t0, nsteps, K, record != 0, store, s2); });
     if (rc) return rc;
     const bool start_perm_id = h->perm_id;
     h->cur = forward_final_slot(h, nsteps, K, record != 0);  // also when the chain ran as a replayed graph
@@ -979,6 +991,7 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
         h->rec_K = K;
         h->rec_resort = nres > 0;
         h->rec_perm_id = start_perm_id;
+        h->rec_store = store;
     }
     return DSTIR_OK;
 }
@@ -1024,15 +1037,30 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
         int L = std::min(K, n - s0);
         float* slot0 = h->ckpt + (size_t)sgi * sf;
         auto slot = [&](int j) -> float* { return j == 0 ? slot0 : h->seg + (size_t)(j - 1) * sf; };
+        // grid slot of substep k of the segment: the segment's own slots, or
+        // the forward's slot s0 + k when the rollout kept its grids
+        const size_t g0 = h->rec_store ? (size_t)s0 : 0;
         auto grids = [&](int k, float4*& pm, float4*& vo) {
-            pm = h->pm + (size_t)k * h->G;
-            vo = h->vo + (size_t)k * h->G;
+            pm = h->pm + (g0 + k) * h->G;
+            vo = h->vo + (g0 + k) * h->G;
         };
-        // recompute the segment, keeping every state and grid; the state after
-        // its last substep is not needed by the adjoint
         h->in_recompute = true;
-        chain_forward(h, t0 + s0, L, slot, grids, h->force_scratch, (long long)h->max_steps * 3, t0 + s0, 0, true,
-                      true, s0, st);
+        if (h->rec_store) {
+            // states only: G2P from the kept velocity grids, with F of the next
+            // state written by G2P since P2G does not run
+            for (int k = 0; k + 1 < L; ++k) {
+                float4 *pm, *vo;
+                grids(k, pm, vo);
+                FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + s0 + k, h->force_scratch,
+                                     (long long)h->max_steps * 3, t0 + s0 + k, 0);
+                timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st, h->tight, true); });
+            }
+        } else {
+            // recompute the segment, keeping every state and grid; the state
+            // after its last substep is not needed by the adjoint
+            chain_forward(h, t0 + s0, L, slot, grids, h->force_scratch, (long long)h->max_steps * 3, t0 + s0, 0, true,
+                          true, s0, st);
+        }
         h->in_recompute = false;
         // adjoint of the state at global step g (relative to t0) lives in A[(n - g) & 1]
         auto adj_args = [&](int k) {
@@ -1042,8 +1070,8 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.gblk = h->gblk;
             a.cur = slot(k);
             a.stride = h->stride;
-            a.pm = h->pm + (size_t)k * h->G;
-            a.vo = h->vo + (size_t)k * h->G;
+            a.pm = h->pm + (g0 + k) * h->G;
+            a.vo = h->vo + (g0 + k) * h->G;
             a.ga = h->ga;
             a.pmb = h->pmb;
             a.adj_next = A[(n - (s0 + k + 1)) & 1];
@@ -1064,7 +1092,8 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.vo2 = nullptr;
             a.adj_prev = nullptr;
             a.box = box_slot(h, s0 + k);
-            a.order = vorder_slot(h, k, true);
+            // the kept-grid path recomputes states without building orders
+            a.order = h->rec_store ? nullptr : vorder_slot(h, k, true);
             return a;
         };
         if (!fused_adj(h)) {
@@ -1084,7 +1113,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
                 timed(h, K_GRID_ADJ, st, [&] { launch_grid_adj(a, h->n_gblocks, h->gblock, st); });
                 if (k >= 1) {
                     a.cur2 = slot(k - 1);
-                    a.vo2 = h->vo + (size_t)(k - 1) * h->G;
+                    a.vo2 = h->vo + (g0 + k - 1) * h->G;
                     a.adj_prev = A[(n - (s0 + k - 1)) & 1];
                     timed(h, K_P2G_ADJ_G2P_ADJ, st,
                           [&] { launch_p2g_adj_g2p_adj(a, h->n_blocks, h->block, var, h->any_svd, st, h->tight); });
@@ -1125,7 +1154,7 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
         if ((rc = dalloc(h, &h->seg, (size_t)K * sf, "segment states"))) return rc;
         h->seg_slots = K;
     }
-    if ((rc = ensure_grid_slots(h, K))) return rc;
+    if (!h->rec_store && (rc = ensure_grid_slots(h, K))) return rc;
     if (binned(h) && (rc = ensure_bin_slots(h, K))) return rc;
     if ((rc = ensure_vorder(h, K))) return rc;
     // dL/dforce [B][n][3] -> internal [B][max_steps][3]
@@ -1133,7 +1162,8 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
                                   (size_t)n * 3 * sizeof(float), (size_t)n * 3 * sizeof(float), (size_t)h->B,
                                   cudaMemcpyDeviceToDevice, st));
     long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant * 16 + h->fuse * 2 + h->fuse_adj,
-                         h->block * 4096 + h->gblock, h->rec_resort ? 1 : 0, vorder_on(h) ? h->reorder : 0};
+                         h->block * 4096 + h->gblock, (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0),
+                         vorder_on(h) ? h->reorder : 0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, [&](cudaStream_t s2) { enqueue_backward(h, s2); });
     if (rc) return rc;
@@ -1185,6 +1215,11 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     }
     if (!strcmp(key, "resort")) {
         h->resort = value ? 1 : 0;
+        h->recorded = false;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "store_grids")) {
+        h->store_grids = value ? 1 : 0;
         h->recorded = false;
         return DSTIR_OK;
     }
@@ -1258,6 +1293,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "tight")) *value = h->tight;
     else if (!strcmp(key, "box")) *value = h->use_box;
     else if (!strcmp(key, "reorder")) *value = h->reorder;
+    else if (!strcmp(key, "store_grids")) *value = h->store_grids;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

@@ -101,7 +101,8 @@ enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_CELL = 2, P2G_BRICK = 3, P2G_WARP = 4 };
 // tight: register-cap level of the particle kernels (0, 1 or 2; see kernels.cu)
 void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st, int tight = 0);
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st);
-void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight = 0);
+// write_f: G2P also writes F of the next state (see g2p_kernel)
+void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight = 0, bool write_f = false);
 // G2P of substep f (into a.next) fused with the stress and P2G scatter of
 // substep f+1 (F into a.next2, grid into a.pm_next)
 void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st,

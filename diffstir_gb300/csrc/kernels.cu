@@ -190,7 +190,10 @@ __global__ void __launch_bounds__(256) grid_kernel(FwdArgs a) {
     }
 }
 
-template <int MINB>
+// WRITE_F: also write F of the next state, F_tmp = (I + dt C) F of the
+// current one (what P2G stores, :39-42, :153), for the reverse pass's state
+// recompute when the P2G grids of the rollout were kept and P2G is not rerun.
+template <int MINB, bool WRITE_F>
 __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
@@ -248,6 +251,21 @@ __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
                 for (int b = 0; b < 3; ++b) nC[q * 3 + b] = c4 * (nC[q * 3 + b] - nv[q] * fx[b]);
         } else {
             atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
+        }
+        if (WRITE_F) {
+            float Cc[9], F[9], Ft[9];
+            load9(a.cur, a.stride, OC, p, Cc);
+            load9(a.cur, a.stride, OF, p, F);
+            if (bi.kind == KIND_LIQUID) {
+                float IC[9];
+#pragma unroll
+                for (int i = 0; i < 9; ++i) IC[i] = s.dt * Cc[i] + ((i % 4 == 0) ? 1.f : 0.f);
+                matmul3(IC, F, Ft);
+            } else {
+#pragma unroll
+                for (int i = 0; i < 9; ++i) Ft[i] = F[i];
+            }
+            store9(a.next, a.stride, OF, p, Ft);
         }
         store9(a.next, a.stride, OC, p, nC);
         float nx[3], outv[3];
@@ -916,12 +934,14 @@ void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svd
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks > 0) grid_kernel<<<n_gblocks, gblock, 0, st>>>(a);
 }
-void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight) {
+void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight, bool write_f) {
     if (n_blocks <= 0) return;
-    if (tight >= 1)
-        g2p_kernel<4><<<n_blocks, block, 0, st>>>(a);
+    if (write_f)
+        g2p_kernel<3, true><<<n_blocks, block, 0, st>>>(a);
+    else if (tight >= 1)
+        g2p_kernel<4, false><<<n_blocks, block, 0, st>>>(a);
     else
-        g2p_kernel<3><<<n_blocks, block, 0, st>>>(a);
+        g2p_kernel<3, false><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;

@@ -70,10 +70,12 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 3, 'graph': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 4, 'resort': 0},
             {'p2g': 4, 'graph': 1}, {'p2g': 4, 'tight': 0}, {'p2g': 4, 'tight': 2},
             {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'tight': 0}, {'p2g': 4, 'reorder': 3},
-            {'p2g': 1, 'reorder': 2, 'graph': 1}]
+            {'p2g': 1, 'reorder': 2, 'graph': 1}, {'p2g': 4, 'store_grids': 1},
+            {'p2g': 4, 'store_grids': 1, 'graph': 1, 'reorder': 3}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
-               'warp-tight0', 'warp-tight2', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph']
+               'warp-tight0', 'warp-tight2', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph', 'warp-store',
+               'warp-store-graph-reorder3']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
@@ -236,6 +238,35 @@ def test_processing_order_matches_fixed_order(opts):
         assert rel(st1[k], st0[k]) < 1e-4, k
         assert rel(ds1[k], ds0[k]) < 1e-3, k
     assert rel(dp1, dp0) < 1e-4
+
+
+@pytest.mark.parametrize('opts', [{'p2g': 4}, {'p2g': 1, 'graph': 1}, {'p2g': 4, 'resort': 0}, {'p2g': 0}],
+                         ids=['warp', 'vec-graph', 'warp-noresort', 'plain'])
+def test_kept_grids_match_recompute(opts):
+    """Keeping every substep's P2G and velocity grids (the reverse pass then
+    recomputes states with G2P alone) gives the forces, gradients and
+    step-0 state adjoint of the full segment recompute; two scenes, twice."""
+    T, K = 30, 8
+    scenes = [rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=12)),
+              rounded(S.small_synthetic_scene(n_grid=20, ppc=4, n_steps=T, seed=13))]
+    wts = torch.as_tensor(np.random.default_rng(7).normal(size=(2, T, 3)), dtype=torch.float32, device='cuda')
+    out = {}
+    for keep in (0, 1):
+        sim = Simulator(scenes, max_steps=T, options=dict(opts, store_grids=keep))
+        for rep in range(2):
+            sim.reset()
+            f = sim.forward(T, ckpt_every=K, record=True).cpu().numpy()
+            dp, ds = sim.backward(wts, want_state0=True)
+            out[(keep, rep)] = (f, dp.cpu().numpy(), {k: v.cpu().numpy() for k, v in ds.items()})
+        assert sim.status() == 0
+        sim.close()
+    f0, dp0, ds0 = out[(0, 0)]
+    for key in ((0, 1), (1, 0), (1, 1)):
+        f, dp, ds = out[key]
+        assert rel(f, f0) < 1e-5
+        assert rel(dp, dp0) < 1e-4
+        for k in 'xvCF':
+            assert rel(ds[k], ds0[k]) < 1e-3, k
 
 
 def test_checkpoint_interval_invariance():
