@@ -90,6 +90,7 @@ def parse():
     ap.add_argument('--no-cpu', action='store_true')
     ap.add_argument('--no-fd', action='store_true', help='skip the central-difference gradient check')
     ap.add_argument('--no-plain', action='store_true', help='skip the plain single-scene comparison')
+    ap.add_argument('--no-kept', action='store_true', help='skip the kept-grids measurement')
     ap.add_argument('--fd-h', type=float, default=1e-3, help='relative step of the gradient check')
     return ap.parse_args()
 
@@ -269,6 +270,7 @@ def run_ours(args):
     dev = torch.device('cuda', local)
     N = sum(s.n_particles for s in scenes)
     B = len(scenes)
+    G_all = sum(s.desc.n_grid ** 3 for s in scenes)
     rng = np.random.default_rng(1000 + rank)
     ys = S_yield(args.config)
 
@@ -340,6 +342,34 @@ def run_ours(args):
     else:
         n_total = float(N)
     value = n_total * T / (ms / 1e3)
+
+    # the same gradient evaluation with every substep's grids kept (option
+    # store_grids: the reverse pass recomputes states with G2P alone), where
+    # they fit in a third of the free device memory; reported beside the
+    # headline value, which recomputes each segment in full
+    kept = None
+    grid_bytes = T * G_all * 32
+    if not args.no_kept and not sim.get_option('store_grids') and grid_bytes < torch.cuda.mem_get_info(dev)[0] / 3:
+        sim.set_option('store_grids', 1)
+        for _ in range(2):
+            grad_eval(params)
+        torch.cuda.synchronize()
+        k0, k1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        k0.record(stream)
+        for _ in range(args.steps):
+            grad_eval(params)
+        k1.record(stream)
+        torch.cuda.synchronize()
+        kms = k0.elapsed_time(k1) / args.steps
+        if world > 1:
+            import torch.distributed as dist
+            t = torch.tensor([kms], device=dev)
+            dist.all_reduce(t, op=dist.ReduceOp.MAX)
+            kms = float(t.item())
+        sim.set_option('store_grids', 0)
+        kept = {'value': n_total * T / (kms / 1e3), 'unit': UNIT, 'ms_per_step': kms, 'grid_memory_gb': grid_bytes / 1e9,
+                'what': 'option store_grids: P2G and velocity grids of all substeps kept; the reverse pass '
+                        'recomputes the states of each 50-substep segment with G2P alone'}
 
     # forward-only rate: the same rollout without recording checkpoints
     sim.set_params(params)
@@ -546,6 +576,7 @@ def run_ours(args):
                          ((T // ckpt + ckpt) * N * 96 / 1e9)},
         'grad_evals_per_s': world * B * 1e3 / ms,
         'forward_value': n_total * T / (fwd_ms / 1e3),
+        'kept_grids': kept,
         'grad_check': grad_check,
         'plain': plain,
         'forward_adjoint_roofline_frac': step_bytes / (ms / 1e3) / 1e9 / hbm,

@@ -1195,13 +1195,21 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     if (!h || !key) return DSTIR_EINVAL;
     if (!strcmp(key, "p2g")) {
         if (value < 0 || value > 4) return fail(h, DSTIR_EINVAL, "p2g variant %lld not in 0..4", (long long)value);
+        if (value == P2G_CELL && h->gblock > 256)
+            return fail(h, DSTIR_EINVAL, "p2g variant 2 needs gblock <= 256");
         h->p2g_variant = (int)value;
         h->recorded = false;
         return DSTIR_OK;
     }
     if (!strcmp(key, "block") || !strcmp(key, "gblock")) {
-        if (value != 64 && value != 128 && value != 256)
-            return fail(h, DSTIR_EINVAL, "%s must be 64, 128 or 256", key);
+        // grid blocks may be larger (fewer partial sums in the rod-force
+        // reduction); the cell-binned kernels run one thread per cell in
+        // blocks of gblock and are built for at most 256
+        const bool grid_key = !strcmp(key, "gblock");
+        if (value != 64 && value != 128 && value != 256 && !(grid_key && (value == 512 || value == 1024)))
+            return fail(h, DSTIR_EINVAL, "%s must be 64, 128 or 256 (gblock also 512 or 1024)", key);
+        if (grid_key && value > 256 && h->p2g_variant == P2G_CELL)
+            return fail(h, DSTIR_EINVAL, "gblock above 256 does not work with p2g variant 2");
         if (!strcmp(key, "block"))
             h->block = (int)value;
         else

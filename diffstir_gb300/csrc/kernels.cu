@@ -126,7 +126,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
         }
 }
 
-__global__ void __launch_bounds__(256) grid_kernel(FwdArgs a) {
+__global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ float sh[32][4];
     __shared__ float rc[3], rc1[3];
@@ -584,7 +584,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
     if (bi.kind == KIND_LIQUID && active) store3(a.adj_cur, a.stride, OX, p, xb);
 }
 
-__global__ void __launch_bounds__(256) grid_adj_kernel(AdjArgs a) {
+__global__ void __launch_bounds__(1024) grid_adj_kernel(AdjArgs a) {
     __shared__ SceneDev s;
     __shared__ float rc[3], rodv[3], fb[3];
     const GridBlock gb = a.gblk[blockIdx.x];
