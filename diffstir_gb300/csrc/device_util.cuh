@@ -88,16 +88,21 @@ __device__ __forceinline__ void red_add4(float4* p, float a, float b, float c, f
 // vector RED:
 //   1. lane L adds lane L-1's k+2 value into its own k+1 value;
 //   2. lane L adds lane L-1's k+1 value (as updated by step 1) into its k+0.
-// A lane whose k+1 and k+2 values were taken by lane L+1 (n1) emits only its
-// k+0 value.  Every value reaches exactly one RED, whatever the keys, so the
-// sums are exact for any particle order; only the number of REDs depends on
-// it (34 instead of 96 per row for a warp on 32 consecutive base cells).
+// When lane L-1 has key-2 instead (flag g1: one empty cell between them, the
+// rows overlap by one node), step 1 adds lane L-1's k+2 value into lane L's
+// k+0 value.  A lane whose k+1 and k+2 values were taken by lane L+1 (n1)
+// emits only its k+0 value; one whose k+2 value alone was taken (ng1) emits
+// k+0 and k+1.  Every value reaches exactly one RED, whatever the keys, so
+// the sums are exact for any particle order; only the number of REDs depends
+// on it (34 instead of 96 per row for a warp on 32 consecutive base cells).
 // Inactive lanes take distinct negative keys and zero values.  All 32 lanes
 // must call these.
 // ---------------------------------------------------------------------------
 struct RunAgg {
     bool a1;    // lane L-1 has key-1: take its k+1 and k+2 values
+    bool g1;    // lane L-1 has key-2: take its k+2 value
     bool n1;    // lane L+1 takes this lane's k+1 and k+2 values
+    bool ng1;   // lane L+1 takes this lane's k+2 value only
     bool any;   // some lane of the warp aggregates
 };
 
@@ -109,8 +114,12 @@ __device__ __forceinline__ RunAgg run_agg_flags(int key) {
     int k1 = __shfl_up_sync(full, key, 1);
     RunAgg r;
     r.a1 = lane >= 1 && k1 == key - 1;
-    r.n1 = __shfl_down_sync(full, (int)r.a1, 1) && lane < 31;
-    r.any = __any_sync(full, r.a1);
+    r.g1 = lane >= 1 && k1 == key - 2;
+    const int flags = (r.a1 ? 1 : 0) | (r.g1 ? 2 : 0);
+    const int nf = __shfl_down_sync(full, flags, 1);
+    r.n1 = lane < 31 && (nf & 1);
+    r.ng1 = lane < 31 && (nf & 2);
+    r.any = __any_sync(full, flags != 0);
     return r;
 }
 
@@ -130,6 +139,11 @@ __device__ __forceinline__ void run_agg_scatter(const RunAgg& r, float4* row, fl
             c1.y += t1;
             c1.z += t2;
             if (NW == 4) c1.w += t3;
+        } else if (r.g1) {
+            c0.x += t0;
+            c0.y += t1;
+            c0.z += t2;
+            if (NW == 4) c0.w += t3;
         }
         t0 = __shfl_up_sync(full, c1.x, 1);
         t1 = __shfl_up_sync(full, c1.y, 1);
@@ -147,7 +161,7 @@ __device__ __forceinline__ void run_agg_scatter(const RunAgg& r, float4* row, fl
     atomicAdd(row, c0);
     if (!r.n1) {
         atomicAdd(row + 1, c1);
-        atomicAdd(row + 2, c2);
+        if (!r.ng1) atomicAdd(row + 2, c2);
     }
 }
 
