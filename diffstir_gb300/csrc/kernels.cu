@@ -126,9 +126,55 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
         }
 }
 
-__global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
+// Reaction force of the moving cylinder (the rod branch of grid_op
+// :212-220 summed as compute_loss :330-336 does for the rod particles): one
+// block per scene walks the nodes of the rod's bounding column in a fixed
+// order and reduces m (v_rod - v) / dt over the nodes inside the cylinder.
+// It reads the P2G grid before grid_kernel clears it; grid_kernel itself then
+// carries no reduction, so its blocks outside the occupied box finish at once.
+__global__ void __launch_bounds__(256) rod_force_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ float sh[32][4];
+    const int scene = blockIdx.x;
+    load_scene_shared(s, a.sc + scene);
+    __syncthreads();
+    if (s.rod_mode != DSTIR_ROD_CYLINDER) return;  // block-uniform
+    const float* t0 = a.traj + ((long long)scene * a.traj_len + a.f) * 3;
+    float rc[3], rodv[3];
+#pragma unroll
+    for (int c = 0; c < 3; ++c) {
+        rc[c] = t0[c];
+        rodv[c] = (t0[3 + c] - t0[c]) / s.dt;
+    }
+    const int n = s.n;
+    const float r = sqrtf(s.rod_r2);
+    // bounding column, one node of slack each way; the cylinder test below
+    // is the grid update's own and decides
+    const int i0 = max(0, (int)floorf((rc[0] - r) * s.inv_dx) - 1), i1 = min(n - 1, (int)ceilf((rc[0] + r) * s.inv_dx) + 1);
+    const int k0 = max(0, (int)floorf((rc[2] - r) * s.inv_dx) - 1), k1 = min(n - 1, (int)ceilf((rc[2] + r) * s.inv_dx) + 1);
+    const int j0 = max(0, (int)floorf(rc[1] * s.inv_dx) - 1);
+    const int ni = i1 - i0 + 1, nk = k1 - k0 + 1, nj = n - j0;
+    const int total = (ni > 0 && nk > 0 && nj > 0) ? ni * nk * nj : 0;
+    float fsum[3] = {0.f, 0.f, 0.f};
+    for (int q = threadIdx.x; q < total; q += blockDim.x) {
+        const int ii = i0 + q / (nj * nk), rem = q % (nj * nk), jj = j0 + rem / nk, kk = k0 + rem % nk;
+        float ex = (float)ii * s.dx - rc[0], ez = (float)kk * s.dx - rc[2];
+        if (ex * ex + ez * ez < s.rod_r2 && (float)jj * s.dx >= rc[1]) {
+            const float4 g = a.pm[s.goff + ((long long)ii * n + jj) * n + kk];
+            const float inv_m = 1.f / (g.w + 1e-10f);
+            fsum[0] += g.w * (rodv[0] - inv_m * g.x) / s.dt;
+            fsum[1] += g.w * (rodv[1] - inv_m * g.y) / s.dt;
+            fsum[2] += g.w * (rodv[2] - inv_m * g.z) / s.dt;
+        }
+    }
+    block_reduce<3>(fsum, sh);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) a.force[scene * a.force_stride + (long long)a.fo * 3 + c] = fsum[c];
+}
+
+__global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
+    __shared__ SceneDev s;
     __shared__ float rc[3], rc1[3];
     // every thread reads the block descriptor (one broadcast load), so the
     // scene copy and the trajectory loads do not wait on a serial chain
@@ -141,7 +187,6 @@ __global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
     }
     __syncthreads();
     long long node = gb.start + threadIdx.x;
-    float fsum[3] = {0.f, 0.f, 0.f};
     const int n = s.n;
     int i, j, k;
     node_ijk((int)(node - s.goff), n, i, j, k);
@@ -174,19 +219,10 @@ __global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
             float ex = (float)i * s.dx - rc[0], ez = (float)k * s.dx - rc[2];
             if (ex * ex + ez * ez < s.rod_r2 && (float)j * s.dx >= rc[1]) {
 #pragma unroll
-                for (int c = 0; c < 3; ++c) {
-                    const float rodv = (rc1[c] - rc[c]) / s.dt;
-                    float u = inv_m * (c == 0 ? g.x : (c == 1 ? g.y : g.z));
-                    fsum[c] = g.w * (rodv - u) / s.dt;
-                    v[c] = rodv;
-                }
+                for (int c = 0; c < 3; ++c) v[c] = (rc1[c] - rc[c]) / s.dt;
             }
         }
         a.vo[node] = make_float4(v[0], v[1], v[2], 0.f);
-    }
-    if (s.rod_mode == DSTIR_ROD_CYLINDER) {
-        group_sum<3>(fsum, sh, a.partial, a.counters + gb.scene, blockIdx.x - gb.idx, gb.count,
-                     a.force + gb.scene * a.force_stride + (long long)a.fo * 3, 1.f);
     }
 }
 
@@ -932,7 +968,9 @@ void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svd
              : p2g_kernel<P2G_VEC, false, 4><<<n_blocks, block, 0, st>>>(a);
 }
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
-    if (n_gblocks > 0) grid_kernel<<<n_gblocks, gblock, 0, st>>>(a);
+    if (n_gblocks <= 0) return;
+    rod_force_kernel<<<a.batch, 256, 0, st>>>(a);  // before grid_kernel clears the P2G grid
+    grid_kernel<<<n_gblocks, gblock, 0, st>>>(a);
 }
 void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight, bool write_f) {
     if (n_blocks <= 0) return;
