@@ -132,7 +132,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
 // order and reduces m (v_rod - v) / dt over the nodes inside the cylinder.
 // It reads the P2G grid before grid_kernel clears it; grid_kernel itself then
 // carries no reduction, so its blocks outside the occupied box finish at once.
-__global__ void __launch_bounds__(256) rod_force_kernel(FwdArgs a) {
+__global__ void __launch_bounds__(1024) rod_force_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ float sh[32][4];
     const int scene = blockIdx.x;
@@ -969,7 +969,7 @@ void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svd
 }
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks <= 0) return;
-    rod_force_kernel<<<a.batch, 256, 0, st>>>(a);  // before grid_kernel clears the P2G grid
+    rod_force_kernel<<<a.batch, 1024, 0, st>>>(a);  // before grid_kernel clears the P2G grid
     grid_kernel<<<n_gblocks, gblock, 0, st>>>(a);
 }
 void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight, bool write_f) {
