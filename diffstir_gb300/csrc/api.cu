@@ -426,7 +426,6 @@ void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot
     } else {
         timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st, h->tight); });
     }
-    ++h->launches;  // launch_grid issues the rod-force and grid kernels
     timed(h, K_GRID, st, [&] { launch_grid(a, h->n_gblocks, h->gblock, st); });
     if (h->p2g_variant == P2G_BRICK && h->brick_gather)
         timed(h, K_G2P, st, [&] {
@@ -724,7 +723,6 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
         grids(k, pm, vo);
         FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + k, force, fstride, fo0 + k, clear_pm);
         a.box = box_slot(h, box0 + k);
-        ++h->launches;  // launch_grid issues the rod-force and grid kernels
         timed(h, K_GRID, st, [&] { launch_grid(a, h->n_gblocks, h->gblock, st); });
         if (k + 1 < nsteps) {
             float4 *pmn, *von;

@@ -42,6 +42,9 @@ struct FwdArgs {
     // processing order of the liquid particles (thread slot q works on particle
     // order[q], a permutation inside each scene's liquid range) or NULL
     const int* order = nullptr;
+    // grid update: blocks [0, n_gblocks) update nodes, the next `batch` blocks
+    // compute the rod reaction force of one scene each (set by launch_grid)
+    int n_gblocks = 0;
 };
 
 struct AdjArgs {

@@ -127,15 +127,23 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
 }
 
 // Reaction force of the moving cylinder (the rod branch of grid_op
-// :212-220 summed as compute_loss :330-336 does for the rod particles): one
-// block per scene walks the nodes of the rod's bounding column in a fixed
-// order and reduces m (v_rod - v) / dt over the nodes inside the cylinder.
-// It reads the P2G grid before grid_kernel clears it; grid_kernel itself then
-// carries no reduction, so its blocks outside the occupied box finish at once.
-__global__ void __launch_bounds__(1024) rod_force_kernel(FwdArgs a) {
-    __shared__ SceneDev s;
-    __shared__ float sh[32][4];
-    const int scene = blockIdx.x;
+// :212-220 summed as compute_loss :330-336 does for the rod particles), run
+// by the extra blocks of grid_kernel, one per scene: the block walks the nodes
+// of the rod's bounding column in a fixed order, reduces m (v_rod - v) / dt
+// over the nodes inside the cylinder and clears their P2G entries (the node
+// blocks leave those to it).  The node blocks carry no reduction, so the ones
+// outside the occupied box finish at once.
+// Node (i, j, k) inside the moving cylinder (grid_op :212-214).  Both the
+// node blocks and the rod-force block classify nodes with this function, in
+// round-to-nearest steps that the compiler may not contract, so the two agree
+// bit for bit on which of them owns a node's P2G entry.
+__device__ __forceinline__ bool in_rod_cylinder(const SceneDev& s, const float rc[3], int i, int j, int k) {
+    const float ex = __fsub_rn(__fmul_rn((float)i, s.dx), rc[0]);
+    const float ez = __fsub_rn(__fmul_rn((float)k, s.dx), rc[2]);
+    return __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ez, ez)) < s.rod_r2 && __fmul_rn((float)j, s.dx) >= rc[1];
+}
+
+__device__ __forceinline__ void rod_force_block(const FwdArgs& a, int scene, SceneDev& s, float (*sh)[4]) {
     load_scene_shared(s, a.sc + scene);
     __syncthreads();
     if (s.rod_mode != DSTIR_ROD_CYLINDER) return;  // block-uniform
@@ -148,8 +156,8 @@ __global__ void __launch_bounds__(1024) rod_force_kernel(FwdArgs a) {
     }
     const int n = s.n;
     const float r = sqrtf(s.rod_r2);
-    // bounding column, one node of slack each way; the cylinder test below
-    // is the grid update's own and decides
+    // bounding column with one node of slack each way; the cylinder test is
+    // the node blocks' own and decides
     const int i0 = max(0, (int)floorf((rc[0] - r) * s.inv_dx) - 1), i1 = min(n - 1, (int)ceilf((rc[0] + r) * s.inv_dx) + 1);
     const int k0 = max(0, (int)floorf((rc[2] - r) * s.inv_dx) - 1), k1 = min(n - 1, (int)ceilf((rc[2] + r) * s.inv_dx) + 1);
     const int j0 = max(0, (int)floorf(rc[1] * s.inv_dx) - 1);
@@ -158,9 +166,10 @@ __global__ void __launch_bounds__(1024) rod_force_kernel(FwdArgs a) {
     float fsum[3] = {0.f, 0.f, 0.f};
     for (int q = threadIdx.x; q < total; q += blockDim.x) {
         const int ii = i0 + q / (nj * nk), rem = q % (nj * nk), jj = j0 + rem / nk, kk = k0 + rem % nk;
-        float ex = (float)ii * s.dx - rc[0], ez = (float)kk * s.dx - rc[2];
-        if (ex * ex + ez * ez < s.rod_r2 && (float)jj * s.dx >= rc[1]) {
-            const float4 g = a.pm[s.goff + ((long long)ii * n + jj) * n + kk];
+        if (in_rod_cylinder(s, rc, ii, jj, kk)) {
+            float4* gp = a.pm + s.goff + ((long long)ii * n + jj) * n + kk;
+            const float4 g = *gp;
+            if (a.clear_pm) *gp = make_float4(0.f, 0.f, 0.f, 0.f);
             const float inv_m = 1.f / (g.w + 1e-10f);
             fsum[0] += g.w * (rodv[0] - inv_m * g.x) / s.dt;
             fsum[1] += g.w * (rodv[1] - inv_m * g.y) / s.dt;
@@ -176,6 +185,11 @@ __global__ void __launch_bounds__(1024) rod_force_kernel(FwdArgs a) {
 __global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
     __shared__ SceneDev s;
     __shared__ float rc[3], rc1[3];
+    __shared__ float sh[32][4];
+    if ((int)blockIdx.x >= a.n_gblocks) {  // block-uniform: a rod-force block
+        rod_force_block(a, (int)blockIdx.x - a.n_gblocks, s, sh);
+        return;
+    }
     // every thread reads the block descriptor (one broadcast load), so the
     // scene copy and the trajectory loads do not wait on a serial chain
     const GridBlock gb = a.gblk[blockIdx.x];
@@ -194,7 +208,10 @@ __global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
     // their P2G entry is still zero and their velocity is never gathered
     if (node < gb.end && (!a.box || box_inside(a.box + gb.scene * 6, i, j, k))) {
         float4 g = a.pm[node];
-        if (a.clear_pm) a.pm[node] = make_float4(0.f, 0.f, 0.f, 0.f);
+        // nodes inside the rod belong to the rod-force block, which reads
+        // and clears their P2G entries (their velocity is the rod's anyway)
+        const bool in_rod = s.rod_mode == DSTIR_ROD_CYLINDER && in_rod_cylinder(s, rc, i, j, k);
+        if (a.clear_pm && !in_rod) a.pm[node] = make_float4(0.f, 0.f, 0.f, 0.f);
         float inv_m = 1.f / (g.w + 1e-10f);
         float v[3] = {inv_m * g.x, inv_m * g.y, inv_m * g.z};
         if (s.container_wall) {  // :204-210
@@ -215,13 +232,9 @@ __global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
         if (k > n - b && v[2] > 0.f) v[2] = 0.f;
         if (j < b && v[1] < 0.f) v[1] = 0.f;
         if (j > n - b && v[1] > 0.f) v[0] = v[1] = v[2] = 0.f;
-        if (s.rod_mode == DSTIR_ROD_CYLINDER) {
-            float ex = (float)i * s.dx - rc[0], ez = (float)k * s.dx - rc[2];
-            if (ex * ex + ez * ez < s.rod_r2 && (float)j * s.dx >= rc[1]) {
+        if (in_rod)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) v[c] = (rc1[c] - rc[c]) / s.dt;
-            }
-        }
+            for (int c = 0; c < 3; ++c) v[c] = (rc1[c] - rc[c]) / s.dt;
         a.vo[node] = make_float4(v[0], v[1], v[2], 0.f);
     }
 }
@@ -674,8 +687,7 @@ __global__ void __launch_bounds__(1024) grid_adj_kernel(AdjArgs a) {
     if (j > n - b && v[1] > 0.f) { mask[0] = mask[1] = mask[2] = 0.f; }
     bool inside = false;
     if (s.rod_mode == DSTIR_ROD_CYLINDER) {
-        float ex = (float)i * s.dx - rc[0], ez = (float)k * s.dx - rc[2];
-        inside = (ex * ex + ez * ez < s.rod_r2 && (float)j * s.dx >= rc[1]);
+        inside = in_rod_cylinder(s, rc, i, j, k);  // the forward's classification
     }
     float ub[3], mb = 0.f;
     if (inside) {
@@ -969,8 +981,9 @@ void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svd
 }
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks <= 0) return;
-    rod_force_kernel<<<a.batch, 1024, 0, st>>>(a);  // before grid_kernel clears the P2G grid
-    grid_kernel<<<n_gblocks, gblock, 0, st>>>(a);
+    FwdArgs b = a;
+    b.n_gblocks = n_gblocks;  // the last `batch` blocks compute the rod forces
+    grid_kernel<<<n_gblocks + a.batch, gblock, 0, st>>>(b);
 }
 void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight, bool write_f) {
     if (n_blocks <= 0) return;
