@@ -109,7 +109,7 @@ struct DstirHandle {
     std::vector<DstirSceneDesc> desc;
     std::vector<SceneDev> sc_h;
     long long N = 0, stride = 0, G = 0;
-    int block = 256, gblock = 256, p2g_variant = P2G_WARP, use_graph = 0;
+    int block = 256, gblock = 1024, p2g_variant = P2G_WARP, use_graph = 0;
     int brick_gather = 1;   // with P2G_BRICK: G2P and the P2G adjoint also gather from brick tiles
     int brick_scatter = 1;  // with P2G_BRICK: 0 shared atomics, 1 shared red, 2 direct global atomics
     int fuse = 0;           // per-particle variants: G2P(f) and P2G(f+1) in one kernel (measured 4% slower at 64^3)
@@ -1195,10 +1195,12 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     if (!h || !key) return DSTIR_EINVAL;
     if (!strcmp(key, "p2g")) {
         if (value < 0 || value > 4) return fail(h, DSTIR_EINVAL, "p2g variant %lld not in 0..4", (long long)value);
-        if (value == P2G_CELL && h->gblock > 256)
-            return fail(h, DSTIR_EINVAL, "p2g variant 2 needs gblock <= 256");
         h->p2g_variant = (int)value;
         h->recorded = false;
+        if (value == P2G_CELL && h->gblock > 256) {  // its cell kernels run in blocks of gblock <= 256
+            h->gblock = 256;
+            return build_tables(h);
+        }
         return DSTIR_OK;
     }
     if (!strcmp(key, "block") || !strcmp(key, "gblock")) {
