@@ -402,19 +402,21 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
                     for (int k = 0; k < 3; ++k) {
                         float4 g = __ldg(a.vo + row + k);
                         float W = wij * w[k][2];
-                        float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
-                        float wg0 = W * g.x, wg1 = W * g.y, wg2 = W * g.z;
-                        nv[0] += wg0;
-                        nv[1] += wg1;
-                        nv[2] += wg2;
-                        nC[0] += wg0 * d0; nC[1] += wg0 * d1; nC[2] += wg0 * d2;
-                        nC[3] += wg1 * d0; nC[4] += wg1 * d1; nC[5] += wg1 * d2;
-                        nC[6] += wg2 * d0; nC[7] += wg2 * d1; nC[8] += wg2 * d2;
+                        float wg[3] = {W * g.x, W * g.y, W * g.z};
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            nv[q] += wg[q];
+                            if (i) nC[q * 3 + 0] += (float)i * wg[q];
+                            if (j) nC[q * 3 + 1] += (float)j * wg[q];
+                            if (k) nC[q * 3 + 2] += (float)k * wg[q];
+                        }
                     }
                 }
             float c4 = 4.f * s.inv_dx;
 #pragma unroll
-            for (int i = 0; i < 9; ++i) nC[i] *= c4;
+            for (int q = 0; q < 3; ++q)
+#pragma unroll
+                for (int b = 0; b < 3; ++b) nC[q * 3 + b] = c4 * (nC[q * 3 + b] - nv[q] * fx[b]);
         } else if (active) {
             atomicOr(a.status, DSTIR_STATUS_OUT_OF_GRID);
         }
@@ -478,6 +480,14 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
         {
             float w[3][3];
             bspline(fx, w);
+            // factored affine momentum, as in p2g_kernel
+            float cc[3], Ad[9];
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                cc[q] = mv[q] - s.dx * (A[q * 3 + 0] * fx[0] + A[q * 3 + 1] * fx[1] + A[q * 3 + 2] * fx[2]);
+#pragma unroll
+                for (int b = 0; b < 3; ++b) Ad[q * 3 + b] = s.dx * A[q * 3 + b];
+            }
             RunAgg ra;
             if (WARP) ra = run_agg_flags(act2 ? (base[0] * s.n + base[1]) * s.n + base[2] : run_agg_inactive_key());
 #pragma unroll
@@ -486,15 +496,16 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
                 for (int j = 0; j < 3; ++j) {
                     float wij = w[i][0] * w[j][1];
                     long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    float r[3];
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) r[q] = cc[q] + (float)i * Ad[q * 3 + 0] + (float)j * Ad[q * 3 + 1];
                     float4 c[3];
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
                         float W = wij * w[k][2];
-                        float dp0 = ((float)i - fx[0]) * s.dx, dp1 = ((float)j - fx[1]) * s.dx,
-                              dp2 = ((float)k - fx[2]) * s.dx;
-                        float g0 = W * (mv[0] + (A[0] * dp0 + A[1] * dp1 + A[2] * dp2));
-                        float g1 = W * (mv[1] + (A[3] * dp0 + A[4] * dp1 + A[5] * dp2));
-                        float g2 = W * (mv[2] + (A[6] * dp0 + A[7] * dp1 + A[8] * dp2));
+                        float g0 = W * (r[0] + (float)k * Ad[2]);
+                        float g1 = W * (r[1] + (float)k * Ad[5]);
+                        float g2 = W * (r[2] + (float)k * Ad[8]);
                         float gm = W * m;
                         float4* dst = a.pm_next + row + k;
                         if (VARIANT == P2G_PLAIN) {
@@ -796,20 +807,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_g2p_adj_kernel(AdjArgs a) {
             if (locate(x, s.inv_dx, s.n, base, fx)) {
                 float w[3][3], dw[3][3];
                 bspline_d(fx, w, dw);
-#pragma unroll
-                for (int i = 0; i < 3; ++i)
-#pragma unroll
-                    for (int j = 0; j < 3; ++j) {
-                        long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
-#pragma unroll
-                        for (int k = 0; k < 3; ++k) {
-                            float dp[3] = {((float)i - fx[0]) * s.dx, ((float)j - fx[1]) * s.dx,
-                                           ((float)k - fx[2]) * s.dx};
-                            p2g_adj_node(w[i][0] * w[j][1] * w[k][2], dw[i][0] * w[j][1] * w[k][2],
-                                         w[i][0] * dw[j][1] * w[k][2], w[i][0] * w[j][1] * dw[k][2], dp,
-                                         __ldg(a.pmb + row + k), m, mv, A, s.dx, liquid, Ab, vvb, fxb);
-                        }
-                    }
+                p2g_adj_gather(a.pmb, s, base, fx, w, dw, m, mv, A, liquid, Ab, vvb, fxb);
             }
             float Fb[9];
             p2g_adj_core<SVDJ>(a, s, prm, model, p, kind, m, Ab, vvb, fxb, pg, xb, vb, Cb, Fb);
@@ -847,8 +845,15 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_g2p_adj_kernel(AdjArgs a) {
         if (in2 || WARP) {
             float w[3][3], dw[3][3];
             bspline_d(fx, w, dw);
+            // factored as in g2p_adj_kernel: vnb + c4 Cb (o - fx) = e + Cc o
             const float c4 = 4.f * s.inv_dx;
-            float fxb[3] = {0.f, 0.f, 0.f};
+            float Cc[9], e[3];
+#pragma unroll
+            for (int q = 0; q < 9; ++q) Cc[q] = c4 * Cb[q];
+#pragma unroll
+            for (int q = 0; q < 3; ++q)
+                e[q] = vnb[q] - (Cc[q * 3 + 0] * fx[0] + Cc[q * 3 + 1] * fx[1] + Cc[q * 3 + 2] * fx[2]);
+            float fxb[3] = {0.f, 0.f, 0.f}, U[3] = {0.f, 0.f, 0.f};
             RunAgg ra;
             if (WARP) ra = run_agg_flags(act2 ? (base[0] * s.n + base[1]) * s.n + base[2] : run_agg_inactive_key());
 #pragma unroll
@@ -856,44 +861,47 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_g2p_adj_kernel(AdjArgs a) {
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
                     long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    const float wij = w[i][0] * w[j][1], dxij = dw[i][0] * w[j][1], dyij = w[i][0] * dw[j][1];
+                    float r[3];
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) r[q] = e[q] + (float)i * Cc[q * 3 + 0] + (float)j * Cc[q * 3 + 1];
                     float4 cw[3];
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        float W = w[i][0] * w[j][1] * w[k][2];
-                        float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
-                        float Cd0 = Cb[0] * d0 + Cb[1] * d1 + Cb[2] * d2;
-                        float Cd1 = Cb[3] * d0 + Cb[4] * d1 + Cb[5] * d2;
-                        float Cd2 = Cb[6] * d0 + Cb[7] * d1 + Cb[8] * d2;
+                        const float W = wij * w[k][2];
+                        const float rk0 = r[0] + (float)k * Cc[2], rk1 = r[1] + (float)k * Cc[5],
+                                    rk2 = r[2] + (float)k * Cc[8];
                         float4* dst = a.ga + row + k;
-                        float g0 = W * (vnb[0] + c4 * Cd0), g1 = W * (vnb[1] + c4 * Cd1),
-                              g2 = W * (vnb[2] + c4 * Cd2);
+                        const float g0 = W * rk0, g1 = W * rk1, g2 = W * rk2;
                         if (VARIANT == P2G_PLAIN) {
-                            float* dd = reinterpret_cast<float*>(dst);
-                            atomicAdd(dd + 0, g0);
-                            atomicAdd(dd + 1, g1);
-                            atomicAdd(dd + 2, g2);
+                            if (act2) {
+                                float* dd = reinterpret_cast<float*>(dst);
+                                atomicAdd(dd + 0, g0);
+                                atomicAdd(dd + 1, g1);
+                                atomicAdd(dd + 2, g2);
+                            }
                         } else if (VARIANT == P2G_VEC) {
-                            red_add4(dst, g0, g1, g2, 0.f);
+                            if (act2) red_add4(dst, g0, g1, g2, 0.f);
                         } else {
                             cw[k] = make_float4(g0, g1, g2, 0.f);
                         }
                         if (liquid) {
-                            float4 g = __ldg(a.vo2 + row + k);
-                            float Wb = vnb[0] * g.x + vnb[1] * g.y + vnb[2] * g.z +
-                                       c4 * (g.x * Cd0 + g.y * Cd1 + g.z * Cd2);
-                            fxb[0] -= c4 * W * (Cb[0] * g.x + Cb[3] * g.y + Cb[6] * g.z);
-                            fxb[1] -= c4 * W * (Cb[1] * g.x + Cb[4] * g.y + Cb[7] * g.z);
-                            fxb[2] -= c4 * W * (Cb[2] * g.x + Cb[5] * g.y + Cb[8] * g.z);
-                            fxb[0] += Wb * dw[i][0] * w[j][1] * w[k][2];
-                            fxb[1] += Wb * w[i][0] * dw[j][1] * w[k][2];
-                            fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
+                            const float4 g = __ldg(a.vo2 + row + k);
+                            const float Wb = g.x * rk0 + g.y * rk1 + g.z * rk2;
+                            U[0] += W * g.x;
+                            U[1] += W * g.y;
+                            U[2] += W * g.z;
+                            fxb[0] += Wb * dxij * w[k][2];
+                            fxb[1] += Wb * dyij * w[k][2];
+                            fxb[2] += Wb * wij * dw[k][2];
                         }
                     }
                     if (WARP) run_agg_scatter<3>(ra, a.ga + row, cw[0], cw[1], cw[2], act2);
                 }
             if (liquid)
 #pragma unroll
-                for (int c = 0; c < 3; ++c) xbo[c] += s.inv_dx * fxb[c];
+                for (int b = 0; b < 3; ++b)
+                    xbo[b] += s.inv_dx * (fxb[b] - (Cc[0 * 3 + b] * U[0] + Cc[1 * 3 + b] * U[1] + Cc[2 * 3 + b] * U[2]));
         }
         if (liquid && active) store3(a.adj_prev, a.stride, OX, p, xbo);
     }
