@@ -84,6 +84,7 @@ def parse():
     ap.add_argument('--box', type=int, default=None, help='1: grid kernels skip nodes outside the occupied box')
     ap.add_argument('--reorder', type=int, default=None, help='processing order rebuilt every N substeps (0: never)')
     ap.add_argument('--store-grids', type=int, default=None, help='1: keep every substep\'s grids, recompute states only')
+    ap.add_argument('--overlap', type=int, default=None, help='1: segment recompute on a second stream')
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')
@@ -258,7 +259,7 @@ def run_ours(args):
     scenes, T, ckpt = build_workload(args, rank)
     sc = scenes[0]
     opts = {}
-    keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather', 'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder', 'store_grids')
+    keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather', 'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder', 'store_grids', 'overlap')
     explicit = any(getattr(args, k) is not None for k in keys)
     if args.autotune and not explicit:
         from diffstir_gb300 import autotune
@@ -586,7 +587,7 @@ def run_ours(args):
         'e2e': e2e,
         'gpu_launches': int(launches),
         'options': {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather',
-                                                   'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder', 'store_grids')},
+                                                   'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder', 'store_grids', 'overlap')},
         'clocks': clk,
         'status_flags': int(st),
     }

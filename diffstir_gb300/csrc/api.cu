@@ -168,6 +168,14 @@ struct DstirHandle {
     int reorder = 0;            // option "reorder": processing order rebuilt every this many substeps (0: never)
     int store_grids = 0;        // option "store_grids": a recorded rollout keeps every substep's grids
     bool rec_store = false;     // the recorded rollout kept its grids
+    // reverse pass: the recompute of segment s-1 runs on rstream while the
+    // adjoint of segment s runs on the caller's stream (double-buffered
+    // segment states and grids, its own partial-sum buffer)
+    int overlap = 1;            // option "overlap"
+    cudaStream_t rstream = nullptr;
+    cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_r[2] = {nullptr, nullptr}, ev_a[2] = {nullptr, nullptr};
+    float* partial2 = nullptr;
+    float* fwd_partial = nullptr;  // partial-sum buffer for the forward kernels being enqueued (NULL: partial)
     int* vord = nullptr;        // [vord_slots][stride] processing orders (slot j: substeps [jR, (j+1)R) of a segment)
     long long vord_slots = 0;
     int* rs_vdest = nullptr;    // [stride] scratch of the processing-order build
@@ -295,6 +303,10 @@ int build_tables(DstirHandle* h) {
     if (pl > h->partial_len) {
         if ((rc = dalloc(h, &h->partial, (size_t)pl * 4, "partial sums"))) return rc;
         h->partial_len = pl;
+        if (h->partial2) {  // the reverse pass reallocates its copy at the new size
+            cudaFree(h->partial2);
+            h->partial2 = nullptr;
+        }
     }
     return DSTIR_OK;
 }
@@ -328,7 +340,7 @@ FwdArgs fwd_args(DstirHandle* h, const float* cur, float* next, float4* pm, floa
     a.force = force;
     a.force_stride = force_stride;
     a.fo = fo;
-    a.partial = h->partial;
+    a.partial = h->fwd_partial ? h->fwd_partial : h->partial;
     a.counters = h->counters;
     a.status = h->status;
     a.clear_pm = clear_pm;
@@ -603,11 +615,19 @@ void dstir_destroy(DstirHandle* h) {
     }
     if (h->ev_in) cudaEventDestroy(h->ev_in);
     if (h->ev_out) cudaEventDestroy(h->ev_out);
+    if (h->rstream) {
+        cudaStreamSynchronize(h->rstream);
+        cudaStreamDestroy(h->rstream);
+    }
+    cudaEvent_t evs[] = {h->ev_fork, h->ev_join, h->ev_r[0], h->ev_r[1], h->ev_a[0], h->ev_a[1]};
+    for (cudaEvent_t e : evs)
+        if (e) cudaEventDestroy(e);
     void* ptrs[] = {h->sc, h->blk, h->gblk, h->work, h->ckpt, h->seg, h->pm, h->vo, h->ga, h->pmb, h->adj,
                     h->traj, h->params, h->models, h->force_scratch, h->pgrad, h->partial, h->counters, h->status,
                     h->cnt, h->bkey, h->brank, h->bsum, h->cell_start, h->perm, h->fbuf, h->dfbuf, h->dpbuf,
                     h->bricks, h->rs_cnt, h->rs_start, h->rs_bsum, h->rs_key, h->rs_rank, h->rs_sorted,
-                    h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0, h->box, h->vord, h->rs_vdest};
+                    h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0, h->box, h->vord, h->rs_vdest,
+                    h->partial2};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -1024,6 +1044,8 @@ namespace {
 // Enqueue the reverse pass of the recorded rollout.  dL/dforce is read from
 // h->dfbuf ([B][max_steps][3], entry fo = substep - t0); dL/dparams goes to
 // h->dpbuf.  Returns the adjoint slot holding dL/d(step-0 state).
+bool overlap_on(const DstirHandle* h) { return h->overlap && !binned(h) && !vorder_on(h); }
+
 int enqueue_backward(DstirHandle* h, cudaStream_t st) {
     const int n = h->rec_n, K = h->rec_K, t0 = h->rec_t0;
     const long long nseg = (n + K - 1) / K;
@@ -1032,19 +1054,28 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
     cudaMemsetAsync(A[0], 0, sf * sizeof(float), st);  // adjoint of the final state: zero
     cudaMemsetAsync(h->ga, 0, (size_t)h->G * sizeof(float4), st);
     cudaMemsetAsync(h->pgrad, 0, (size_t)n * h->B * 4 * sizeof(float), st);
-    for (long long sgi = nseg - 1; sgi >= 0; --sgi) {
-        int s0 = (int)(sgi * K);
-        int L = std::min(K, n - s0);
-        float* slot0 = h->ckpt + (size_t)sgi * sf;
-        auto slot = [&](int j) -> float* { return j == 0 ? slot0 : h->seg + (size_t)(j - 1) * sf; };
-        // grid slot of substep k of the segment: the segment's own slots, or
-        // the forward's slot s0 + k when the rollout kept its grids
-        const size_t g0 = h->rec_store ? (size_t)s0 : 0;
+    const bool ovl = overlap_on(h) && nseg >= 2;
+    // buffer b of the segment states (K-1 slots) and grids (K slots); with the
+    // overlap, segment sgi uses buffer sgi & 1
+    auto buf = [&](long long sgi) -> int { return ovl ? (int)(sgi & 1) : 0; };
+    auto seg_slot = [&](long long sgi, int j) -> float* {
+        return j == 0 ? h->ckpt + (size_t)sgi * sf : h->seg + ((size_t)buf(sgi) * K + (j - 1)) * sf;
+    };
+    // grid slot of substep k of segment sgi: the segment's own slots, or the
+    // forward's slot s0 + k when the rollout kept its grids
+    auto grid_slot = [&](long long sgi, int k) -> size_t {
+        return h->rec_store ? (size_t)(sgi * K + k) : (size_t)buf(sgi) * K + k;
+    };
+    auto recompute = [&](long long sgi, cudaStream_t s) {
+        const int s0 = (int)(sgi * K);
+        const int L = std::min(K, n - s0);
+        auto slot = [&](int j) -> float* { return seg_slot(sgi, j); };
         auto grids = [&](int k, float4*& pm, float4*& vo) {
-            pm = h->pm + (g0 + k) * h->G;
-            vo = h->vo + (g0 + k) * h->G;
+            pm = h->pm + grid_slot(sgi, k) * h->G;
+            vo = h->vo + grid_slot(sgi, k) * h->G;
         };
         h->in_recompute = true;
+        if (ovl) h->fwd_partial = h->partial2;
         if (h->rec_store) {
             // states only: G2P from the kept velocity grids, with F of the next
             // state written by G2P since P2G does not run
@@ -1053,15 +1084,21 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
                 grids(k, pm, vo);
                 FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + s0 + k, h->force_scratch,
                                      (long long)h->max_steps * 3, t0 + s0 + k, 0);
-                timed(h, K_G2P, st, [&] { launch_g2p(a, h->n_blocks, h->block, st, h->tight, true); });
+                timed(h, K_G2P, s, [&] { launch_g2p(a, h->n_blocks, h->block, s, h->tight, true); });
             }
         } else {
             // recompute the segment, keeping every state and grid; the state
             // after its last substep is not needed by the adjoint
             chain_forward(h, t0 + s0, L, slot, grids, h->force_scratch, (long long)h->max_steps * 3, t0 + s0, 0, true,
-                          true, s0, st);
+                          true, s0, s);
         }
+        h->fwd_partial = nullptr;
         h->in_recompute = false;
+    };
+    auto adjoint = [&](long long sgi, cudaStream_t s) {
+        const int s0 = (int)(sgi * K);
+        const int L = std::min(K, n - s0);
+        auto slot = [&](int j) -> float* { return seg_slot(sgi, j); };
         // adjoint of the state at global step g (relative to t0) lives in A[(n - g) & 1]
         auto adj_args = [&](int k) {
             AdjArgs a;
@@ -1070,8 +1107,8 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.gblk = h->gblk;
             a.cur = slot(k);
             a.stride = h->stride;
-            a.pm = h->pm + (g0 + k) * h->G;
-            a.vo = h->vo + (g0 + k) * h->G;
+            a.pm = h->pm + grid_slot(sgi, k) * h->G;
+            a.vo = h->vo + grid_slot(sgi, k) * h->G;
             a.ga = h->ga;
             a.pmb = h->pmb;
             a.adj_next = A[(n - (s0 + k + 1)) & 1];
@@ -1097,7 +1134,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             return a;
         };
         if (!fused_adj(h)) {
-            for (int k = L - 1; k >= 0; --k) run_adj_substep(h, adj_args(k), st, k);
+            for (int k = L - 1; k >= 0; --k) run_adj_substep(h, adj_args(k), s, k);
         } else {
             // G2P adjoint of the segment's last substep, then per substep k the
             // grid adjoint and the P2G adjoint of k fused with the G2P adjoint of
@@ -1106,31 +1143,60 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             const int var = h->p2g_variant;  // P2G_PLAIN, P2G_VEC or P2G_WARP here
             {
                 AdjArgs a = adj_args(L - 1);
-                timed(h, K_G2P_ADJ, st, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, st, h->tight); });
+                timed(h, K_G2P_ADJ, s, [&] { launch_g2p_adj(a, h->n_blocks, h->block, var, s, h->tight); });
             }
             for (int k = L - 1; k >= 0; --k) {
                 AdjArgs a = adj_args(k);
-                timed(h, K_GRID_ADJ, st, [&] { launch_grid_adj(a, h->n_gblocks, h->gblock, st); });
+                timed(h, K_GRID_ADJ, s, [&] { launch_grid_adj(a, h->n_gblocks, h->gblock, s); });
                 if (k >= 1) {
                     a.cur2 = slot(k - 1);
-                    a.vo2 = h->vo + (g0 + k - 1) * h->G;
+                    a.vo2 = h->vo + grid_slot(sgi, k - 1) * h->G;
                     a.adj_prev = A[(n - (s0 + k - 1)) & 1];
-                    timed(h, K_P2G_ADJ_G2P_ADJ, st,
-                          [&] { launch_p2g_adj_g2p_adj(a, h->n_blocks, h->block, var, h->any_svd, st, h->tight); });
+                    timed(h, K_P2G_ADJ_G2P_ADJ, s,
+                          [&] { launch_p2g_adj_g2p_adj(a, h->n_blocks, h->block, var, h->any_svd, s, h->tight); });
                 } else {
-                    timed(h, K_P2G_ADJ, st, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, st, h->tight); });
+                    timed(h, K_P2G_ADJ, s, [&] { launch_p2g_adj(a, h->n_blocks, h->block, h->any_svd, s, h->tight); });
                 }
             }
         }
         if (h->rec_resort && sgi > 0) {
             // checkpoint sgi was re-sorted from the state that ended segment
-            // sgi-1: bring the adjoint of state s0 back to that order
+            // sgi-1: bring the adjoint of state s0 back to that order (through
+            // the other adjoint slot, whose state s0+1 adjoint is spent)
             float* adj0 = A[(n - s0) & 1];
-            timed(h, K_OTHER, st, [&] {
-                launch_unpermute(adj0, h->seg, h->rs_dest + (size_t)sgi * h->stride, h->stride, h->N, st);
+            float* tmp = A[(n - s0 + 1) & 1];
+            timed(h, K_OTHER, s, [&] {
+                launch_unpermute(adj0, tmp, h->rs_dest + (size_t)sgi * h->stride, h->stride, h->N, s);
             });
-            cudaMemcpyAsync(adj0, h->seg, sf * sizeof(float), cudaMemcpyDeviceToDevice, st);
+            cudaMemcpyAsync(adj0, tmp, sf * sizeof(float), cudaMemcpyDeviceToDevice, s);
         }
+    };
+    if (!ovl) {
+        for (long long sgi = nseg - 1; sgi >= 0; --sgi) {
+            recompute(sgi, st);
+            adjoint(sgi, st);
+        }
+    } else {
+        // software pipeline over the two streams: the recompute of segment
+        // sgi-1 (rstream) overlaps the adjoint of segment sgi (st); it reuses
+        // the buffers of segment sgi+1, so it waits for that adjoint first
+        cudaStream_t rs = h->rstream;
+        cudaEventRecord(h->ev_fork, st);
+        cudaStreamWaitEvent(rs, h->ev_fork, 0);
+        recompute(nseg - 1, rs);
+        cudaEventRecord(h->ev_r[(nseg - 1) & 1], rs);
+        for (long long sgi = nseg - 1; sgi >= 0; --sgi) {
+            if (sgi >= 1) {
+                if (sgi + 1 <= nseg - 1) cudaStreamWaitEvent(rs, h->ev_a[(sgi + 1) & 1], 0);
+                recompute(sgi - 1, rs);
+                cudaEventRecord(h->ev_r[(sgi - 1) & 1], rs);
+            }
+            cudaStreamWaitEvent(st, h->ev_r[sgi & 1], 0);
+            adjoint(sgi, st);
+            cudaEventRecord(h->ev_a[sgi & 1], st);
+        }
+        cudaEventRecord(h->ev_join, rs);
+        cudaStreamWaitEvent(st, h->ev_join, 0);
     }
     cudaMemsetAsync(h->pm, 0, (size_t)h->G * sizeof(float4), st);
     timed(h, K_OTHER, st, [&] { launch_reduce_pgrad(h->pgrad, n, h->B, h->dpbuf, st); });
@@ -1150,11 +1216,22 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
     const int n = h->rec_n, K = h->rec_K;
     size_t sf = slot_floats(h);
     int rc;
-    if (K > h->seg_slots) {
-        if ((rc = dalloc(h, &h->seg, (size_t)K * sf, "segment states"))) return rc;
-        h->seg_slots = K;
+    const bool ovl = overlap_on(h) && (n + K - 1) / K >= 2;
+    const long long nbuf = ovl ? 2 : 1;
+    if (nbuf * K > h->seg_slots) {
+        if ((rc = dalloc(h, &h->seg, (size_t)(nbuf * K) * sf, "segment states"))) return rc;
+        h->seg_slots = nbuf * K;
     }
-    if (!h->rec_store && (rc = ensure_grid_slots(h, K))) return rc;
+    if (!h->rec_store && (rc = ensure_grid_slots(h, nbuf * K))) return rc;
+    if (ovl) {
+        if (!h->rstream) {
+            CUDA_TRY(h, cudaStreamCreateWithFlags(&h->rstream, cudaStreamNonBlocking));
+            cudaEvent_t* evs[] = {&h->ev_fork, &h->ev_join, &h->ev_r[0], &h->ev_r[1], &h->ev_a[0], &h->ev_a[1]};
+            for (cudaEvent_t* e : evs) CUDA_TRY(h, cudaEventCreateWithFlags(e, cudaEventDisableTiming));
+        }
+        if (!h->partial2 && (rc = dalloc(h, &h->partial2, (size_t)h->partial_len * 4, "recompute partial sums")))
+            return rc;
+    }
     if (binned(h) && (rc = ensure_bin_slots(h, K))) return rc;
     if ((rc = ensure_vorder(h, K))) return rc;
     // dL/dforce [B][n][3] -> internal [B][max_steps][3]
@@ -1162,7 +1239,8 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
                                   (size_t)n * 3 * sizeof(float), (size_t)n * 3 * sizeof(float), (size_t)h->B,
                                   cudaMemcpyDeviceToDevice, st));
     long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant * 16 + h->fuse * 2 + h->fuse_adj,
-                         h->block * 4096 + h->gblock, (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0),
+                         h->block * 4096 + h->gblock,
+                         (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0) + (ovl ? 4 : 0),
                          vorder_on(h) ? h->reorder : 0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, [&](cudaStream_t s2) { enqueue_backward(h, s2); });
@@ -1226,6 +1304,10 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     if (!strcmp(key, "resort")) {
         h->resort = value ? 1 : 0;
         h->recorded = false;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "overlap")) {
+        h->overlap = value ? 1 : 0;
         return DSTIR_OK;
     }
     if (!strcmp(key, "store_grids")) {
@@ -1304,6 +1386,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "box")) *value = h->use_box;
     else if (!strcmp(key, "reorder")) *value = h->reorder;
     else if (!strcmp(key, "store_grids")) *value = h->store_grids;
+    else if (!strcmp(key, "overlap")) *value = h->overlap;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

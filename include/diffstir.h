@@ -161,7 +161,10 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * re-sort alone at 64^3), "store_grids" [0] (a recorded rollout keeps
  * the P2G and velocity grids of every substep, 32 bytes per grid node and
  * substep, and the reverse pass recomputes the states of each segment with
- * G2P alone instead of rerunning P2G and the grid update), "brick_scatter" /
+ * G2P alone instead of rerunning P2G and the grid update), "overlap" [1] (the
+ * reverse pass recomputes segment s-1 on a second stream while it runs the
+ * adjoint of segment s; per-particle variants without "reorder"),
+ * "brick_scatter" /
  * "brick_gather" (scatter and gather forms of variant 3), "profile" [0] (1:
  * time every launch with CUDA events; totals via dstir_get_option
  * "prof_ns:<kernel>" / "prof_count:<kernel>"), "launches" (reset the launch

@@ -269,6 +269,37 @@ def test_kept_grids_match_recompute(opts):
             assert rel(ds[k], ds0[k]) < 1e-3, k
 
 
+@pytest.mark.parametrize('opts', [{'p2g': 4}, {'p2g': 4, 'graph': 1}, {'p2g': 4, 'store_grids': 1},
+                                  {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 0, 'resort': 0}],
+                         ids=['warp', 'warp-graph', 'warp-kept', 'warp-fused', 'plain'])
+def test_overlapped_reverse_pass_matches_serial(opts):
+    """The reverse pass with the segment recompute on a second stream
+    (overlapping the adjoint of the next segment) gives the serial pass's
+    forces, gradients and step-0 state adjoint; two scenes, seven segments,
+    twice in a row."""
+    T, K = 34, 5
+    scenes = [rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=14)),
+              rounded(S.small_synthetic_scene(n_grid=20, ppc=4, n_steps=T, seed=15))]
+    wts = torch.as_tensor(np.random.default_rng(8).normal(size=(2, T, 3)), dtype=torch.float32, device='cuda')
+    out = {}
+    for ovl in (0, 1):
+        sim = Simulator(scenes, max_steps=T, options=dict(opts, overlap=ovl))
+        for rep in range(2):
+            sim.reset()
+            f = sim.forward(T, ckpt_every=K, record=True).cpu().numpy()
+            dp, ds = sim.backward(wts, want_state0=True)
+            out[(ovl, rep)] = (f, dp.cpu().numpy(), {k: v.cpu().numpy() for k, v in ds.items()})
+        assert sim.status() == 0
+        sim.close()
+    f0, dp0, ds0 = out[(0, 0)]
+    for key in ((0, 1), (1, 0), (1, 1)):
+        f, dp, ds = out[key]
+        assert rel(f, f0) < 1e-5
+        assert rel(dp, dp0) < 1e-4
+        for k in 'xvCF':
+            assert rel(ds[k], ds0[k]) < 1e-3, k
+
+
 def test_checkpoint_interval_invariance():
     T = 24
     sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=4))
