@@ -209,6 +209,7 @@ struct DstirHandle {
     cudaEvent_t ev_in = nullptr, ev_out = nullptr;
     cudaGraphExec_t fwd_exec = nullptr, bwd_exec = nullptr;
     long long fwd_key[8] = {0}, bwd_key[8] = {0};
+    long long fwd_kernels = 0, bwd_kernels = 0;  // kernel launches in one replay of each graph
 
     int cur = 0;  // work slot holding the current state
     bool in_recompute = false;  // profiler: launches belong to a segment recompute
@@ -924,7 +925,7 @@ int enqueue_forward(DstirHandle* h, int t0, int nsteps, int K, bool record, bool
 // replayed on the library stream (ordered after / before `st` by events).
 template <class Body>
 int run_maybe_graph(DstirHandle* h, cudaStream_t st, cudaGraphExec_t* exec, long long* key, const long long* want,
-                    Body body) {
+                    long long* graph_kernels, Body body) {
     if (!h->use_graph) {
         body(st);
         CUDA_TRY(h, cudaGetLastError());
@@ -943,7 +944,10 @@ int run_maybe_graph(DstirHandle* h, cudaStream_t st, cudaGraphExec_t* exec, long
         cudaGraph_t g = nullptr;
         CUDA_TRY(h, cudaStreamBeginCapture(h->gstream, cudaStreamCaptureModeThreadLocal));
         h->capturing = true;
+        const long long before = h->launches;
         body(h->gstream);
+        *graph_kernels = h->launches - before;  // kernels per replay; capturing launches none
+        h->launches = before;
         h->capturing = false;
         cudaError_t e = cudaStreamEndCapture(h->gstream, &g);
         if (e != cudaSuccess) return fail(h, DSTIR_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
@@ -958,6 +962,7 @@ int run_maybe_graph(DstirHandle* h, cudaStream_t st, cudaGraphExec_t* exec, long
     CUDA_TRY(h, cudaEventRecord(h->ev_in, st));
     CUDA_TRY(h, cudaStreamWaitEvent(h->gstream, h->ev_in, 0));
     CUDA_TRY(h, cudaGraphLaunch(*exec, h->gstream));
+    h->launches += *graph_kernels;
     CUDA_TRY(h, cudaEventRecord(h->ev_out, h->gstream));
     CUDA_TRY(h, cudaStreamWaitEvent(st, h->ev_out, 0));
     return DSTIR_OK;
@@ -994,7 +999,7 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
                          h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0) + (vorder_on(h) ? 512 * h->reorder : 0) +
                              (store ? (1LL << 40) : 0),
                          h->block * 4096 + h->gblock};
-    rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want,
+    rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want, &h->fwd_kernels,
                          [&](cudaStream_t s2) { enqueue_forward(h, t0, nsteps, K, record != 0, store, s2); });
     if (rc) return rc;
     const bool start_perm_id = h->perm_id;
@@ -1243,7 +1248,8 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
                          (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0) + (ovl ? 4 : 0),
                          vorder_on(h) ? h->reorder : 0};
     int final_nx = n % 2;
-    rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, [&](cudaStream_t s2) { enqueue_backward(h, s2); });
+    rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, &h->bwd_kernels,
+                         [&](cudaStream_t s2) { enqueue_backward(h, s2); });
     if (rc) return rc;
     float* A[2] = {h->adj, h->adj + sf};
     if (dL_dparams)

@@ -341,6 +341,13 @@ def test_graph_replay_matches_eager_and_is_reusable():
         torch.cuda.synchronize()
         assert rel(fg.cpu().numpy(), fe.cpu().numpy()) < 1e-5
         assert rel(gg.cpu().numpy(), ge.cpu().numpy()) < 1e-4
+    # the launch counter counts the kernels inside each replayed graph
+    for sim in (eager, graph):
+        sim.reset()
+        sim.set_option('launches', 0)
+        sim.forward(T, ckpt_every=5, record=True)
+        sim.backward(wts)
+    assert graph.get_option('launches') == eager.get_option('launches') > 0
 
 
 def test_batched_equals_single():
