@@ -85,6 +85,7 @@ def parse():
     ap.add_argument('--reorder', type=int, default=None, help='processing order rebuilt every N substeps (0: never)')
     ap.add_argument('--store-grids', type=int, default=None, help='1: keep every substep\'s grids, recompute states only')
     ap.add_argument('--overlap', type=int, default=None, help='1: segment recompute on a second stream')
+    ap.add_argument('--lsort', type=int, default=None, help='1: re-interleave each block before the warp scatters')
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')
@@ -161,15 +162,33 @@ def peaks():
         return 6800.0, 'fallback'
 
 
-def ncu_traffic(kernel, workload):
-    """dram bytes per launch of `kernel` from the committed ncu summary, if any."""
+def ncu_value(name, kernel, workload):
+    """`name[kernel@workload] = value` from the committed ncu summaries, if any."""
     for path in glob.glob(os.path.join(ROOT, 'profiles', '*.md')) + glob.glob(os.path.join(ROOT, 'profiles', '*.txt')):
         txt = open(path).read()
-        m = re.search(r'traffic_bytes_per_launch\[%s@%s\]\s*[:=]\s*([0-9.eE+]+)' % (re.escape(kernel), re.escape(workload)),
+        m = re.search(r'%s\[%s@%s\]\s*[:=]\s*([0-9.eE+]+)' % (re.escape(name), re.escape(kernel), re.escape(workload)),
                       txt)
         if m:
             return float(m.group(1))
     return None
+
+
+def ncu_traffic(kernel, workload):
+    """dram bytes per launch of `kernel` from the committed ncu summary, if any."""
+    return ncu_value('traffic_bytes_per_launch', kernel, workload)
+
+
+def red_peak(G):
+    """Vector-RED sectors/s this GPU retires on an L2-resident grid of G nodes
+    (dstir_measure_red_rate), or None."""
+    import ctypes
+    import torch
+    from diffstir_gb300 import _lib
+    rate = ctypes.c_double(0.0)
+    torch.cuda.synchronize()
+    rc = _lib.lib().dstir_measure_red_rate(max(int(G), 1 << 18), 256, ctypes.byref(rate),
+                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return rate.value if rc == 0 else None
 
 
 def build_workload(args, rank):
@@ -259,7 +278,8 @@ def run_ours(args):
     scenes, T, ckpt = build_workload(args, rank)
     sc = scenes[0]
     opts = {}
-    keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather', 'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder', 'store_grids', 'overlap')
+    keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather', 'fuse', 'fuse_adj', 'resort', 'tight',
+            'box', 'reorder', 'store_grids', 'overlap', 'lsort')
     explicit = any(getattr(args, k) is not None for k in keys)
     if args.autotune and not explicit:
         from diffstir_gb300 import autotune
@@ -554,6 +574,22 @@ def run_ours(args):
             'frac': achieved / hbm, 'peak_kind': peak_kind, 'alg_bytes_per_launch': alg,
             'avg_launch_us': avg_s * 1e6, 'traffic': ncu_traffic(dom, args.config),
             'launches_per_step': cnt}
+    # atomic roofline of the two scatter kernels: vector-RED sectors per launch
+    # (committed ncu summary) over the live mean launch time, against the RED
+    # sector rate measured on this GPU
+    red_roof = None
+    if sim.get_option('p2g') in (1, 4) and not sim.get_option('fuse'):
+        peak_red = red_peak(G)
+        red_roof = {'unit': 'RED sectors/s', 'peak': peak_red,
+                    'peak_kind': 'measured: 32 consecutive float4 nodes per warp RED, L2-resident grid'}
+        for k in ('p2g', 'g2p_adj'):
+            t_ms, c = both[k]
+            if not c:
+                continue
+            sec = ncu_value('red_sectors_per_launch', k, args.config)
+            ach = sec / (t_ms / 1e3 / c) if sec else None
+            red_roof[k] = {'sectors_per_launch': sec, 'avg_launch_us': t_ms / c * 1e3, 'achieved': ach,
+                           'frac': ach / peak_red if (ach and peak_red) else None}
     # whole-step algorithmic bytes: forward 192 N + 56 G, adjoint 480 N + 112 G per substep
     step_bytes = T * ((192 + 480) * N + (56 + 112) * G)
     kernel_share = {k: round(prof[k][0] / max(sum(v[0] for v in prof.values()), 1e-9), 4) for k in KERNELS}
@@ -583,11 +619,13 @@ def run_ours(args):
         'forward_adjoint_roofline_frac': step_bytes / (ms / 1e3) / 1e9 / hbm,
         'roofline': roof,
         'kernel_time_share': kernel_share,
+        'roofline_l2_red': red_roof,
         'cpu_baseline': cpu,
         'e2e': e2e,
         'gpu_launches': int(launches),
         'options': {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather',
-                                                   'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder', 'store_grids', 'overlap')},
+                                                   'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder', 'store_grids', 'overlap',
+                                                   'lsort')},
         'clocks': clk,
         'status_flags': int(st),
     }

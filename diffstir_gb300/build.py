@@ -1,6 +1,6 @@
 """In-tree build of the CUDA extension libdiffstir.so for sm_103a.
 
-The three translation units under csrc/ are compiled in parallel with nvcc
+The translation units under csrc/ are compiled in parallel with nvcc
 (``-gencode arch=compute_103a,code=sm_103a``) and linked into
 ``diffstir_gb300/_build/libdiffstir.so``, a plain shared library exporting the
 C ABI of include/diffstir.h.  No torch headers are involved.
@@ -15,7 +15,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(HERE, 'csrc')
 OUT_DIR = os.path.join(HERE, '_build')
 LIB = os.path.join(OUT_DIR, 'libdiffstir.so')
-SOURCES = ['kernels.cu', 'binning.cu', 'svd.cu', 'api.cu', 'static_substep.cu', 'resort.cu']
+SOURCES = ['kernels.cu', 'binning.cu', 'svd.cu', 'api.cu', 'static_substep.cu', 'resort.cu', 'calib.cu']
 HEADERS = ['common.cuh', 'svd.cuh', 'device_util.cuh', 'adjoint.cuh', 'internal.h']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
 NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2',

@@ -167,6 +167,7 @@ struct DstirHandle {
     int use_box = 1;            // option "box": the grid kernels skip nodes outside the occupied box
     int reorder = 0;            // option "reorder": processing order rebuilt every this many substeps (0: never)
     int store_grids = 0;        // option "store_grids": a recorded rollout keeps every substep's grids
+    int lsort = 1;              // option "lsort": warp-aggregated scatters re-interleave each block's particles
     bool rec_store = false;     // the recorded rollout kept its grids
     // reverse pass: the recompute of segment s-1 runs on rstream while the
     // adjoint of segment s runs on the caller's stream (double-buffered
@@ -348,6 +349,7 @@ FwdArgs fwd_args(DstirHandle* h, const float* cur, float* next, float4* pm, floa
     a.batch = h->B;
     a.next2 = nullptr;
     a.pm_next = nullptr;
+    a.lsort = h->lsort;
     return a;
 }
 
@@ -997,7 +999,7 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
     if (store && (rc = ensure_grid_slots(h, nsteps))) return rc;
     long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch,
                          h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0) + (vorder_on(h) ? 512 * h->reorder : 0) +
-                             (store ? (1LL << 40) : 0),
+                             (store ? (1LL << 40) : 0) + (h->lsort ? (1LL << 41) : 0),
                          h->block * 4096 + h->gblock};
     rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want, &h->fwd_kernels,
                          [&](cudaStream_t s2) { enqueue_forward(h, t0, nsteps, K, record != 0, store, s2); });
@@ -1136,6 +1138,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.box = box_slot(h, s0 + k);
             // the kept-grid path recomputes states without building orders
             a.order = h->rec_store ? nullptr : vorder_slot(h, k, true);
+            a.lsort = h->lsort;
             return a;
         };
         if (!fused_adj(h)) {
@@ -1245,7 +1248,7 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
                                   cudaMemcpyDeviceToDevice, st));
     long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant * 16 + h->fuse * 2 + h->fuse_adj,
                          h->block * 4096 + h->gblock,
-                         (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0) + (ovl ? 4 : 0),
+                         (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0) + (ovl ? 4 : 0) + (h->lsort ? 8 : 0),
                          vorder_on(h) ? h->reorder : 0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, &h->bwd_kernels,
@@ -1314,6 +1317,10 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     }
     if (!strcmp(key, "overlap")) {
         h->overlap = value ? 1 : 0;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "lsort")) {
+        h->lsort = value ? 1 : 0;
         return DSTIR_OK;
     }
     if (!strcmp(key, "store_grids")) {
@@ -1393,6 +1400,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "reorder")) *value = h->reorder;
     else if (!strcmp(key, "store_grids")) *value = h->store_grids;
     else if (!strcmp(key, "overlap")) *value = h->overlap;
+    else if (!strcmp(key, "lsort")) *value = h->lsort;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

@@ -166,6 +166,140 @@ __device__ __forceinline__ void run_agg_scatter(const RunAgg& r, float4* row, fl
 }
 
 // ---------------------------------------------------------------------------
+// CTA-local re-interleave (option "lsort")
+//
+// The run aggregation above relies on the lanes of a warp holding particles
+// of consecutive base cells of one grid row, the order the periodic re-sort
+// sets up.  As particles cross cell faces between re-sorts that order decays
+// and the number of RED sectors of a 64^3 scene grows from 4.4 M right after a
+// re-sort to 10.5 M fifty substeps later (CPU replay of the scatter on the
+// FP64 trajectory).  Rebuilding the same (row, rank, k) order inside each CTA
+// over its own particles, before the scatter, holds it at 4.8 M one substep
+// and 6.4 M fifty substeps after the re-sort.  The block's lanes then process
+// the block's particles in that order; only which lane handles which particle
+// changes, so the sums are the same up to the order of the float additions.
+//
+//   key   base cell of the particle (clamped into the grid)
+//   rank  its index among the block's particles of that cell: a leader per
+//         group of equal keys in a warp (__match_any_sync) adds the group's
+//         size to the cell's counter in a shared-memory hash table
+//   sort  composite (row - lowest row of the block, rank, k, thread) as one
+//         32-bit word, bitonic-sorted over the block (in-warp steps through
+//         shuffles, the others through shared memory)
+// All threads of the block must call it.
+// ---------------------------------------------------------------------------
+struct LocalOrderSmem {
+    union {
+        struct {
+            int key[512];
+            int cnt[512];
+        } h;
+        unsigned sortbuf[2][256];
+    };
+    int rowmin;
+};
+
+__device__ __forceinline__ unsigned lsort_hash(int key) { return ((unsigned)key * 2654435761u) >> 23; }
+
+// Bitonic sort (ascending) of one distinct 32-bit word per thread over a block
+// of N threads; returns this thread's word of the sorted sequence.  Steps of
+// stride < 32 exchange through shuffles, the others through shared memory
+// (two buffers, one barrier per step).  Fully unrolled for a compile-time N.
+template <int N>
+__device__ __forceinline__ unsigned block_bitonic_sort(unsigned v, unsigned (*buf)[256]) {
+    const unsigned full = 0xffffffffu;
+    const int t = threadIdx.x;
+    int b = 0;
+#pragma unroll
+    for (int size = 2; size <= N; size <<= 1) {
+#pragma unroll
+        for (int st = size >> 1; st > 0; st >>= 1) {
+            unsigned o;
+            if (st >= 32) {
+                buf[b][t] = v;
+                __syncthreads();
+                o = buf[b][t ^ st];
+                b ^= 1;
+            } else {
+                o = __shfl_xor_sync(full, v, st);
+            }
+            const bool take_min = ((t & size) == 0) == ((t & st) == 0);
+            v = take_min ? min(v, o) : max(v, o);
+        }
+    }
+    return v;
+}
+
+// Returns the block-relative particle slot this thread processes; slots
+// holding no particle (>= count) sort last.  N == blockDim.x.
+template <int N>
+__device__ __forceinline__ int local_interleave(const float* cur, long long stride, long long start, int count,
+                                                float inv_dx, int n, LocalOrderSmem& sm) {
+    const unsigned full = 0xffffffffu;
+    const int t = threadIdx.x, lane = t & 31;
+#pragma unroll
+    for (int i = t; i < 512; i += N) {
+        sm.h.key[i] = -1;
+        sm.h.cnt[i] = 0;
+    }
+    if (t == 0) sm.rowmin = INT_MAX;
+    const bool valid = t < count;
+    int b[3] = {0, 0, 0};
+    if (valid) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            const float X = __ldg(cur + (long long)(OX + c) * stride + start + t) * inv_dx - 0.5f;
+            // fmaxf maps NaN to 0, so a corrupt position still gets a cell
+            b[c] = (int)fminf(fmaxf(X, 0.f), (float)(n - 1));
+        }
+    }
+    const int row = b[0] * n + b[1];
+    const int key = valid ? row * n + b[2] : -1 - lane;  // invalid lanes: distinct, never inserted
+    __syncthreads();
+    const int wmin = __reduce_min_sync(full, valid ? row : INT_MAX);
+    if (lane == 0 && wmin != INT_MAX) atomicMin(&sm.rowmin, wmin);
+    const unsigned peers = __match_any_sync(full, key);
+    const int leader = __ffs(peers) - 1;
+    int base_rank = 0;
+    if (valid && lane == leader) {
+        unsigned h = lsort_hash(key);
+        // at most N distinct keys in 512 >= 2N slots: a free or matching slot
+        // is always found within 512 probes
+        for (int probe = 0; probe < 512; ++probe, h = (h + 1) & 511u) {
+            const int old = atomicCAS(&sm.h.key[h], -1, key);
+            if (old == -1 || old == key) {
+                base_rank = atomicAdd(&sm.h.cnt[h], __popc(peers));
+                break;
+            }
+        }
+    }
+    base_rank = __shfl_sync(full, base_rank, leader);
+    const int rank = base_rank + __popc(peers & ((1u << lane) - 1u));
+    __syncthreads();  // rowmin final; the hash table is dead from here on
+    unsigned v;
+    if (valid) {
+        const unsigned rrel = (unsigned)min(row - sm.rowmin, 510);
+        v = (rrel << 23) | ((unsigned)min(rank, 31) << 18) | ((unsigned)b[2] << 8) | (unsigned)t;
+    } else {
+        v = 0xFFFFFF00u | (unsigned)t;
+    }
+    v = block_bitonic_sort<N>(v, sm.sortbuf);
+    return (int)(v & 0xFFu);
+}
+
+// Dispatch on the block size (64, 128 or 256 threads); any other size keeps
+// the block order.
+__device__ __forceinline__ int local_interleave_any(const float* cur, long long stride, long long start, int count,
+                                                    float inv_dx, int n, LocalOrderSmem& sm) {
+    switch (blockDim.x) {
+        case 256: return local_interleave<256>(cur, stride, start, count, inv_dx, n, sm);
+        case 128: return local_interleave<128>(cur, stride, start, count, inv_dx, n, sm);
+        case 64: return local_interleave<64>(cur, stride, start, count, inv_dx, n, sm);
+        default: return threadIdx.x;
+    }
+}
+
+// ---------------------------------------------------------------------------
 // occupied node box of a scene
 //
 // box[0..2] = -(lowest stencil node index) per axis, box[3..5] = highest, all

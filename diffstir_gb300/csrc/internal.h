@@ -45,6 +45,9 @@ struct FwdArgs {
     // grid update: blocks [0, n_gblocks) update nodes, the next `batch` blocks
     // compute the rod reaction force of one scene each (set by launch_grid)
     int n_gblocks = 0;
+    // warp-aggregated P2G: rebuild the interleaved order inside each block of
+    // liquid particles before the scatter (ignored with `order`)
+    int lsort = 0;
 };
 
 struct AdjArgs {
@@ -77,6 +80,7 @@ struct AdjArgs {
     float* adj_prev = nullptr;       // adjoint slot of state f-1 (receives its position-adjoint part)
     const int* box = nullptr;        // occupied node box of substep f (see FwdArgs::box) or NULL
     const int* order = nullptr;      // processing order (see FwdArgs::order) or NULL
+    int lsort = 0;                   // warp-aggregated G2P adjoint: see FwdArgs::lsort
 };
 
 // Counting sort of the particles of one substep by stencil-base cell.

@@ -40,6 +40,14 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
     bool active = p < bi.end;
     if (!active) p = bi.end - 1;  // the lane computes a copy and writes nothing
     if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
+    if constexpr (WARP) {
+        __shared__ LocalOrderSmem lo;
+        if (a.lsort && !a.order && bi.kind == KIND_LIQUID) {
+            p = bi.start + local_interleave_any(a.cur, a.stride, bi.start, (int)(bi.end - bi.start), s.inv_dx, s.n, lo);
+            active = p < bi.end;
+            if (!active) p = bi.end - 1;
+        }
+    }
     float x[3], v[3], C[9];
     load3(a.cur, a.stride, OX, p, x);
     load3(a.cur, a.stride, OV, p, v);
@@ -553,6 +561,14 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
     if (!WARP && !active) return;
     if (!active) p = bi.end - 1;  // WARP: the lane computes a copy and scatters nothing
     if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
+    if constexpr (WARP) {
+        __shared__ LocalOrderSmem lo;
+        if (a.lsort && !a.order && bi.kind == KIND_LIQUID) {
+            p = bi.start + local_interleave_any(a.cur, a.stride, bi.start, (int)(bi.end - bi.start), s.inv_dx, s.n, lo);
+            active = p < bi.end;
+            if (!active) p = bi.end - 1;
+        }
+    }
     float x[3];
     load3(a.cur, a.stride, OX, p, x);
     float xb[3] = {0.f, 0.f, 0.f}, vnb[3], Cb[9];

@@ -164,7 +164,10 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * G2P alone instead of rerunning P2G and the grid update), "overlap" [1] (the
  * reverse pass recomputes segment s-1 on a second stream while it runs the
  * adjoint of segment s; per-particle variants without "reorder"),
- * "brick_scatter" /
+ * "lsort" [1] (variant 4: each block of liquid particles rebuilds the
+ * interleaved order over its own particles before the P2G scatter and the
+ * G2P-adjoint scatter, so the lane-to-lane summation keeps working as
+ * particles drift between re-sorts), "brick_scatter" /
  * "brick_gather" (scatter and gather forms of variant 3), "profile" [0] (1:
  * time every launch with CUDA events; totals via dstir_get_option
  * "prof_ns:<kernel>" / "prof_count:<kernel>"), "launches" (reset the launch
@@ -200,6 +203,14 @@ int dstir_svd3_backward(const float* gU, const float* gS, const float* gV, const
  *    capture.  Device status flags are not reported. */
 int dstir_substep_static(const DstirSceneDesc* scene, const float* params, const float* traj2,
                          const float* state_in, float* state_out, float* force_out, void* stream);
+
+/* Diagnostics, no counterpart in the reference: the rate at which this GPU
+ * retires 16-byte vector float reductions (red.global.add.v4.f32) when each
+ * warp instruction covers 32 consecutive grid nodes (16 sectors of 32 bytes)
+ * of an L2-resident grid of n_nodes nodes.  This is the roofline of the
+ * warp-aggregated P2G and G2P-adjoint scatters.  Allocates and frees its own
+ * grid; synchronises the stream.  sectors_per_s: host pointer. */
+int dstir_measure_red_rate(int64_t n_nodes, int32_t reps, double* sectors_per_s, void* stream);
 
 #ifdef __cplusplus
 }

@@ -71,11 +71,12 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 4, 'graph': 1}, {'p2g': 4, 'tight': 0}, {'p2g': 4, 'tight': 2},
             {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'tight': 0}, {'p2g': 4, 'reorder': 3},
             {'p2g': 1, 'reorder': 2, 'graph': 1}, {'p2g': 4, 'store_grids': 1},
-            {'p2g': 4, 'store_grids': 1, 'graph': 1, 'reorder': 3}]
+            {'p2g': 4, 'store_grids': 1, 'graph': 1, 'reorder': 3}, {'p2g': 4, 'lsort': 0},
+            {'p2g': 4, 'block': 128}, {'p2g': 4, 'block': 64, 'graph': 1}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
                'warp-tight0', 'warp-tight2', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph', 'warp-store',
-               'warp-store-graph-reorder3']
+               'warp-store-graph-reorder3', 'warp-nolsort', 'warp-block128', 'warp-block64-graph']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
@@ -178,6 +179,39 @@ def test_resort_matches_fixed_order(opts):
         assert rel(dp, dp0) < 1e-4
         for k in 'xvCF':
             assert rel(ds[k], ds0[k]) < 1e-3, k
+
+
+@pytest.mark.parametrize('block', [256, 128, 64])
+def test_local_interleave_matches_block_order(block):
+    """Rebuilding the interleaved order inside each block before the warp
+    scatters (option lsort) only changes which lane handles which particle:
+    forces, final state, parameter gradient and the adjoint of the step-0
+    state match the run in block order.  Two scenes of 8 particles per cell
+    (full and partial blocks), long segments so that the particles drift far
+    from the re-sorted order."""
+    T, K = 60, 30
+    scenes = [rounded(S.small_synthetic_scene(n_grid=24, ppc=8, n_steps=T, seed=12)),
+              rounded(S.small_synthetic_scene(n_grid=20, ppc=4, n_steps=T, seed=13))]
+    wts = torch.as_tensor(np.random.default_rng(6).normal(size=(2, T, 3)), dtype=torch.float32, device='cuda')
+    out = {}
+    for ls in (0, 1):
+        sim = Simulator(scenes, max_steps=T, options={'p2g': 4, 'lsort': ls, 'block': block})
+        assert sim.get_option('lsort') == ls
+        sim.reset()
+        f = sim.forward(T, ckpt_every=K, record=True).cpu().numpy()
+        st = {k: v.cpu().numpy() for k, v in sim.get_state().items()}
+        dp, ds = sim.backward(wts, want_state0=True)
+        out[ls] = (f, st, dp.cpu().numpy(), {k: v.cpu().numpy() for k, v in ds.items()})
+        assert sim.status() == 0
+        sim.close()
+    f0, st0, dp0, ds0 = out[0]
+    f, st, dp, ds = out[1]
+    assert rel(f, f0) < 1e-5
+    for k in 'xvCF':
+        assert rel(st[k], st0[k]) < 1e-4, k
+    assert rel(dp, dp0) < 1e-4
+    for k in 'xvCF':
+        assert rel(ds[k], ds0[k]) < 1e-3, k
 
 
 @pytest.mark.parametrize('opts', [{'p2g': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 0},
