@@ -2,7 +2,8 @@
 
 For a scene shape (grid size, particle count, batch, rod mode, J mode) it times
 a short recorded forward + adjoint for each candidate configuration
-(P2G variant, particle block size, grid block size, CUDA-graph replay) with
+(P2G variant, particle block size, grid block size, register caps,
+per-block re-interleave, CUDA-graph replay) with
 CUDA events and keeps the fastest.  Results are cached in a JSON file keyed by
 GPU name and scene shape, so a shape is tuned once per machine.
 
@@ -26,6 +27,7 @@ CANDIDATES = [
     {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 1, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 0},
+    {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1, 'lsort': 0},
     {'p2g': 1, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 3, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 256, 'graph': 0, 'brick_scatter': 2,
      'brick_gather': 0},
@@ -47,7 +49,7 @@ def shape_key(scenes):
     rod = scenes[0].desc.rod_mode
     svd = int(any(s.desc.j_mode == 1 for s in scenes))
     name = torch.cuda.get_device_name() if torch.cuda.is_available() else 'cpu'
-    return 'v8|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
+    return 'v9|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
 
 
 def _load():
