@@ -179,7 +179,7 @@ def ncu_traffic(kernel, workload):
 
 
 def red_peak(G):
-    """Vector-RED sectors/s this GPU retires on an L2-resident grid of G nodes
+    """Vector-RED sectors/s this GPU retires on a grid of G nodes
     (dstir_measure_red_rate), or None."""
     import ctypes
     import torch
@@ -579,7 +579,7 @@ def run_ours(args):
     # sector rate measured on this GPU
     red_roof = None
     if sim.get_option('p2g') in (1, 4) and not sim.get_option('fuse'):
-        peak_red = red_peak(G)
+        peak_red = red_peak(max(s.desc.n_grid ** 3 for s in scenes))  # one scene's grid: L2-resident
         red_roof = {'unit': 'RED sectors/s', 'peak': peak_red,
                     'peak_kind': 'measured: 32 consecutive float4 nodes per warp RED, L2-resident grid'}
         for k in ('p2g', 'g2p_adj'):

@@ -28,6 +28,9 @@ CANDIDATES = [
     {'p2g': 4, 'fuse': 1, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 0},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1, 'lsort': 0},
+    # small scenes fill few SMs with 256-particle blocks
+    {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 128, 'gblock': 256, 'graph': 1, 'tight': 1},
+    {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 64, 'gblock': 256, 'graph': 1, 'tight': 1, 'lsort': 0},
     {'p2g': 1, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 3, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 256, 'graph': 0, 'brick_scatter': 2,
      'brick_gather': 0},
