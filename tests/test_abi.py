@@ -35,3 +35,11 @@ def test_python_prototypes_cover_header():
 def test_scene_desc_layout_matches_header():
     # 10 int32 + 12 float32
     assert ctypes.sizeof(_abi.DstirSceneDesc) == 10 * 4 + 12 * 4
+
+
+def test_red_rate_probe_rejects_bad_arguments_before_any_cuda_call():
+    lib = _abi.bind(ctypes.CDLL(build()))
+    rate = ctypes.c_double(0.0)
+    assert lib.dstir_measure_red_rate(16, 8, ctypes.byref(rate), None) == -1
+    assert lib.dstir_measure_red_rate(1 << 18, 0, ctypes.byref(rate), None) == -1
+    assert lib.dstir_measure_red_rate(1 << 18, 8, None, None) == -1

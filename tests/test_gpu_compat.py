@@ -153,3 +153,15 @@ def test_clip_identification_carries_state():
         for r in res:
             assert r['status'] == 0 and np.isfinite(r['best_loss'])
         assert res[0]['best_loss'] < res[0]['history'][0].min()
+
+
+@pytest.mark.gpu
+def test_red_rate_probe_measures_a_positive_rate():
+    """The vector-RED probe behind the scatter kernels' atomic roofline runs
+    on the current stream and reports a plausible rate (sectors/s)."""
+    import ctypes
+    from diffstir_gb300 import _lib
+    rate = ctypes.c_double(0.0)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert _lib.lib().dstir_measure_red_rate(1 << 18, 64, ctypes.byref(rate), s) == 0
+    assert 1e9 < rate.value < 1e13, rate.value
