@@ -119,6 +119,45 @@ def test_cylinder_scene_parity(model, params, j_mode, opts):
     assert rel(ds_g['F'].reshape(-1, 9), ds_o[:, 15:24]) < 1e-2
 
 
+@pytest.mark.parametrize('opts', [{'p2g': 4}, {'p2g': 4, 'graph': 1, 'tight': 2}, {'p2g': 1, 'lsort': 0}],
+                         ids=['warp', 'warp-graph-tight2', 'vec'])
+def test_state_adjoint_dot_product_vs_fp64(opts):
+    """Dot-product test of the GPU reverse pass against FP64: for a random
+    direction u over all 24 components of a step-0 state with nonzero v, C
+    and F - I, <J^T w, u> from the GPU adjoint (re-sorted segments) equals
+    <w, J u> from central differences of the FP64 oracle along u."""
+    T, K = 24, 6
+    sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=14))
+    rng = np.random.default_rng(15)
+    wts = rng.normal(size=(T, 3))
+    x0 = sc.x0()
+    n = x0.shape[0]
+    v0 = rng.normal(scale=0.05, size=(n, 3)).astype(np.float32).astype(np.float64)
+    C0 = rng.normal(scale=0.2, size=(n, 9)).astype(np.float32).astype(np.float64)
+    F0 = (np.tile(np.eye(3).reshape(1, 9), (n, 1)) + rng.normal(scale=0.01, size=(n, 9))).astype(np.float32)
+    F0 = F0.astype(np.float64)
+    sim = Simulator(sc, max_steps=T, options=opts)
+    sim.set_initial_state(*(torch.as_tensor(a, dtype=torch.float32, device='cuda') for a in (x0, v0, C0, F0)))
+    sim.forward(T, ckpt_every=K, record=True)
+    _, ds = sim.backward(torch.as_tensor(wts[None], dtype=torch.float32, device='cuda'), want_state0=True)
+    assert sim.status() == 0
+    g = np.concatenate([ds['x'].cpu().numpy().reshape(n, 3), ds['v'].cpu().numpy().reshape(n, 3),
+                        ds['C'].cpu().numpy().reshape(n, 9), ds['F'].cpu().numpy().reshape(n, 9)], 1)
+    sim.close()
+    u = rng.normal(size=(n, 24))
+    u[:, :3] *= 1e-2
+    h = 1e-6
+
+    def proj(sign):
+        f, _, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, x0 + sign * h * u[:, :3],
+                                 v0 + sign * h * u[:, 3:6], C0 + sign * h * u[:, 6:15], F0 + sign * h * u[:, 15:])
+        return float((wts * f).sum())
+
+    jvp = (proj(1) - proj(-1)) / (2 * h)
+    vjp = float((g * u).sum())
+    assert abs(vjp - jvp) <= 2e-4 * abs(jvp), (vjp, jvp)  # FP32 oracle on the CPU: 2e-6
+
+
 def test_forward_states_match_oracle():
     T = 30
     sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=4, n_steps=T, seed=2))

@@ -74,6 +74,38 @@ def test_cylinder_scene_state_grad_fd():
             assert abs(ds[p, c] - fd) <= 1e-4 * max(abs(fd), np.abs(ds[:, :3]).max() * 1e-2), (p, c, ds[p, c], fd)
 
 
+@pytest.mark.parametrize('j_mode', [S.J_DET, S.J_SVD])
+def test_state_adjoint_dot_product(j_mode):
+    """Dot-product test of the whole reverse pass on the FP64 oracle: for a
+    random direction u over all 24 components (x, v, C, F) of every
+    particle's step-0 state, <w, J u> by central differences of the forces
+    along u equals <J^T w, u> from the adjoint of the step-0 state."""
+    T = 10
+    sc = S.small_synthetic_scene(n_grid=12, ppc=2, n_steps=T, seed=8, dt=5e-4, j_mode=j_mode)
+    rng = np.random.default_rng(11)
+    wts = rng.normal(size=(T, 3))
+    x0 = sc.x0()
+    n = x0.shape[0]
+    v0 = rng.normal(scale=0.05, size=(n, 3))
+    C0 = rng.normal(scale=0.2, size=(n, 9))
+    F0 = np.tile(np.eye(3).reshape(1, 9), (n, 1)) + rng.normal(scale=0.01, size=(n, 9))
+    _, _, ds, st = oracle.grad(sc.desc, sc.params, sc.trajectory, T, x0, wts, v0, C0, F0, want_state0=True)
+    assert st == 0
+    u = rng.normal(size=(n, 24))
+    u[:, :3] *= 1e-2  # positions: keep the perturbed stencils comparable to the others
+    h = 1e-6
+
+    def proj(sign):
+        f, _, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, x0 + sign * h * u[:, :3],
+                                 v0 + sign * h * u[:, 3:6], C0 + sign * h * u[:, 6:15], F0 + sign * h * u[:, 15:])
+        return float((wts * f).sum())
+
+    jvp = (proj(1) - proj(-1)) / (2 * h)
+    vjp = float((ds * u).sum())
+    assert abs(jvp) > 0
+    assert abs(vjp - jvp) <= 1e-6 * abs(jvp), (vjp, jvp)
+
+
 def test_reference_scene_param_grad_fd():
     """Reference scene (container, rod particles, k=20000), L1 loss as compute_loss."""
     T = 6
