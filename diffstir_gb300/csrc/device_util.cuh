@@ -71,6 +71,19 @@ __device__ __forceinline__ void group_sum(float (&v)[NV], float (*sh)[4], float*
     }
 }
 
+// Programmatic dependent launch (option "pdl").  The substep kernels are
+// launched with programmatic stream serialisation, so a kernel's blocks may
+// become resident while the kernel before it in the stream is still running.
+// Each of them therefore waits, before its first access to device memory,
+// until the grids it depends on have completed and their writes are visible
+// (griddepcontrol.wait; without the launch attribute it returns at once), and
+// then lets the next kernel of the stream be launched (launch_dependents:
+// that kernel's own wait still holds it until this grid has completed).
+__device__ __forceinline__ void pdl_enter() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+    asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
+}
+
 __device__ __forceinline__ void red_add4(float4* p, float a, float b, float c, float d) {
     atomicAdd(p, make_float4(a, b, c, d));
 }

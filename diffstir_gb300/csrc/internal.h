@@ -48,6 +48,8 @@ struct FwdArgs {
     // warp-aggregated P2G: rebuild the interleaved order inside each block of
     // liquid particles before the scatter (ignored with `order`)
     int lsort = 0;
+    // launch with programmatic dependent launch (see pdl_enter)
+    int pdl = 0;
 };
 
 struct AdjArgs {
@@ -81,6 +83,7 @@ struct AdjArgs {
     const int* box = nullptr;        // occupied node box of substep f (see FwdArgs::box) or NULL
     const int* order = nullptr;      // processing order (see FwdArgs::order) or NULL
     int lsort = 0;                   // warp-aggregated G2P adjoint: see FwdArgs::lsort
+    int pdl = 0;                     // see FwdArgs::pdl
 };
 
 // Counting sort of the particles of one substep by stencil-base cell.

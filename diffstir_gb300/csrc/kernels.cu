@@ -27,6 +27,7 @@ namespace dstir {
 // ---------------------------------------------------------------------------
 template <int VARIANT, bool SVDJ, int MINB>
 __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
+    pdl_enter();
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ int boxsh[8][6];
@@ -191,6 +192,7 @@ __device__ __forceinline__ void rod_force_block(const FwdArgs& a, int scene, Sce
 }
 
 __global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
+    pdl_enter();
     __shared__ SceneDev s;
     __shared__ float rc[3], rc1[3];
     __shared__ float sh[32][4];
@@ -252,6 +254,7 @@ __global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
 // recompute when the P2G grids of the rollout were kept and P2G is not rerun.
 template <int MINB, bool WRITE_F>
 __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
+    pdl_enter();
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
@@ -367,6 +370,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
 // particle state and a launch per substep.
 template <int VARIANT, bool SVDJ, int MINB>
 __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
+    pdl_enter();
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
@@ -545,6 +549,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
 // ---------------------------------------------------------------------------
 template <int VARIANT, int MINB>
 __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
+    pdl_enter();
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float fb[3];
@@ -661,6 +666,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
 }
 
 __global__ void __launch_bounds__(1024) grid_adj_kernel(AdjArgs a) {
+    pdl_enter();
     __shared__ SceneDev s;
     __shared__ float rc[3], rodv[3], fb[3];
     const GridBlock gb = a.gblk[blockIdx.x];
@@ -740,6 +746,7 @@ __global__ void __launch_bounds__(1024) grid_adj_kernel(AdjArgs a) {
 // P2G adjoint, one thread per particle (pieces in adjoint.cuh).
 template <bool SVDJ, int MINB>
 __global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
+    pdl_enter();
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
@@ -785,6 +792,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
 // position-adjoint part of f-1 are stored.
 template <int VARIANT, bool SVDJ, int MINB>
 __global__ void __launch_bounds__(256, MINB) p2g_adj_g2p_adj_kernel(AdjArgs a) {
+    pdl_enter();
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
@@ -988,90 +996,102 @@ __global__ void reduce_pgrad_kernel(const float* pgrad, int T, int B, float* out
 // adjoints); level 1 caps G2P and the fused forward at 64 and the adjoints at
 // 80 registers (a few spilled bytes, half again as many resident warps);
 // level 2 also caps P2G at 48.
+// Launch with programmatic stream serialisation when `pdl` is set (the
+// kernels' pdl_enter keeps the ordering), else a plain launch.
+template <class Args>
+void klaunch(void (*k)(Args), unsigned grid, unsigned block, cudaStream_t st, const Args& a) {
+    if (!a.pdl) {
+        k<<<grid, block, 0, st>>>(a);
+        return;
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(block);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    cudaLaunchKernelEx(&cfg, k, a);
+}
+
 void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;
     const bool t2 = tight >= 2 && !svdj;
+    void (*k)(FwdArgs);
     if (variant == P2G_PLAIN)
-        svdj ? p2g_kernel<P2G_PLAIN, true, 4><<<n_blocks, block, 0, st>>>(a)
-             : p2g_kernel<P2G_PLAIN, false, 4><<<n_blocks, block, 0, st>>>(a);
+        k = svdj ? p2g_kernel<P2G_PLAIN, true, 4> : p2g_kernel<P2G_PLAIN, false, 4>;
     else if (variant == P2G_WARP)
-        svdj ? p2g_kernel<P2G_WARP, true, 4><<<n_blocks, block, 0, st>>>(a)
-        : t2 ? p2g_kernel<P2G_WARP, false, 5><<<n_blocks, block, 0, st>>>(a)
-             : p2g_kernel<P2G_WARP, false, 4><<<n_blocks, block, 0, st>>>(a);
+        k = svdj ? p2g_kernel<P2G_WARP, true, 4> : t2 ? p2g_kernel<P2G_WARP, false, 5> : p2g_kernel<P2G_WARP, false, 4>;
     else
-        svdj ? p2g_kernel<P2G_VEC, true, 4><<<n_blocks, block, 0, st>>>(a)
-        : t2 ? p2g_kernel<P2G_VEC, false, 5><<<n_blocks, block, 0, st>>>(a)
-             : p2g_kernel<P2G_VEC, false, 4><<<n_blocks, block, 0, st>>>(a);
+        k = svdj ? p2g_kernel<P2G_VEC, true, 4> : t2 ? p2g_kernel<P2G_VEC, false, 5> : p2g_kernel<P2G_VEC, false, 4>;
+    klaunch(k, n_blocks, block, st, a);
 }
 void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks <= 0) return;
     FwdArgs b = a;
     b.n_gblocks = n_gblocks;  // the last `batch` blocks compute the rod forces
-    grid_kernel<<<n_gblocks + a.batch, gblock, 0, st>>>(b);
+    klaunch(grid_kernel, n_gblocks + a.batch, gblock, st, b);
 }
 void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight, bool write_f) {
     if (n_blocks <= 0) return;
-    if (write_f)
-        g2p_kernel<3, true><<<n_blocks, block, 0, st>>>(a);
-    else if (tight >= 1)
-        g2p_kernel<4, false><<<n_blocks, block, 0, st>>>(a);
-    else
-        g2p_kernel<3, false><<<n_blocks, block, 0, st>>>(a);
+    void (*k)(FwdArgs) = write_f ? g2p_kernel<3, true> : tight >= 1 ? g2p_kernel<4, false> : g2p_kernel<3, false>;
+    klaunch(k, n_blocks, block, st, a);
 }
 void launch_g2p_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;
     const bool t1 = tight >= 1;
+    void (*k)(FwdArgs);
     if (variant == P2G_PLAIN)
-        svdj ? g2p_p2g_kernel<P2G_PLAIN, true, 3><<<n_blocks, block, 0, st>>>(a)
-             : g2p_p2g_kernel<P2G_PLAIN, false, 3><<<n_blocks, block, 0, st>>>(a);
+        k = svdj ? g2p_p2g_kernel<P2G_PLAIN, true, 3> : g2p_p2g_kernel<P2G_PLAIN, false, 3>;
     else if (variant == P2G_WARP)
-        svdj ? g2p_p2g_kernel<P2G_WARP, true, 3><<<n_blocks, block, 0, st>>>(a)
-        : t1 ? g2p_p2g_kernel<P2G_WARP, false, 4><<<n_blocks, block, 0, st>>>(a)
-             : g2p_p2g_kernel<P2G_WARP, false, 3><<<n_blocks, block, 0, st>>>(a);
+        k = svdj ? g2p_p2g_kernel<P2G_WARP, true, 3>
+            : t1 ? g2p_p2g_kernel<P2G_WARP, false, 4>
+                 : g2p_p2g_kernel<P2G_WARP, false, 3>;
     else
-        svdj ? g2p_p2g_kernel<P2G_VEC, true, 3><<<n_blocks, block, 0, st>>>(a)
-        : t1 ? g2p_p2g_kernel<P2G_VEC, false, 4><<<n_blocks, block, 0, st>>>(a)
-             : g2p_p2g_kernel<P2G_VEC, false, 3><<<n_blocks, block, 0, st>>>(a);
+        k = svdj ? g2p_p2g_kernel<P2G_VEC, true, 3>
+            : t1 ? g2p_p2g_kernel<P2G_VEC, false, 4>
+                 : g2p_p2g_kernel<P2G_VEC, false, 3>;
+    klaunch(k, n_blocks, block, st, a);
 }
 void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;
     const bool t1 = tight >= 1;
+    void (*k)(AdjArgs);
     if (variant == P2G_PLAIN)
-        g2p_adj_kernel<P2G_PLAIN, 2><<<n_blocks, block, 0, st>>>(a);
+        k = g2p_adj_kernel<P2G_PLAIN, 2>;
     else if (variant == P2G_WARP)
-        t1 ? g2p_adj_kernel<P2G_WARP, 3><<<n_blocks, block, 0, st>>>(a)
-           : g2p_adj_kernel<P2G_WARP, 2><<<n_blocks, block, 0, st>>>(a);
+        k = t1 ? g2p_adj_kernel<P2G_WARP, 3> : g2p_adj_kernel<P2G_WARP, 2>;
     else
-        t1 ? g2p_adj_kernel<P2G_VEC, 3><<<n_blocks, block, 0, st>>>(a)
-           : g2p_adj_kernel<P2G_VEC, 2><<<n_blocks, block, 0, st>>>(a);
+        k = t1 ? g2p_adj_kernel<P2G_VEC, 3> : g2p_adj_kernel<P2G_VEC, 2>;
+    klaunch(k, n_blocks, block, st, a);
 }
 void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
-    if (n_gblocks > 0) grid_adj_kernel<<<n_gblocks, gblock, 0, st>>>(a);
+    if (n_gblocks > 0) klaunch(grid_adj_kernel, n_gblocks, gblock, st, a);
 }
 void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;
-    if (svdj)
-        p2g_adj_kernel<true, 2><<<n_blocks, block, 0, st>>>(a);
-    else if (tight >= 1)
-        p2g_adj_kernel<false, 3><<<n_blocks, block, 0, st>>>(a);
-    else
-        p2g_adj_kernel<false, 2><<<n_blocks, block, 0, st>>>(a);
+    void (*k)(AdjArgs) = svdj ? p2g_adj_kernel<true, 2> : tight >= 1 ? p2g_adj_kernel<false, 3> : p2g_adj_kernel<false, 2>;
+    klaunch(k, n_blocks, block, st, a);
 }
 void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st,
                             int tight) {
     if (n_blocks <= 0) return;
     const bool t1 = tight >= 1;
+    void (*k)(AdjArgs);
     if (variant == P2G_PLAIN)
-        svdj ? p2g_adj_g2p_adj_kernel<P2G_PLAIN, true, 2><<<n_blocks, block, 0, st>>>(a)
-             : p2g_adj_g2p_adj_kernel<P2G_PLAIN, false, 2><<<n_blocks, block, 0, st>>>(a);
+        k = svdj ? p2g_adj_g2p_adj_kernel<P2G_PLAIN, true, 2> : p2g_adj_g2p_adj_kernel<P2G_PLAIN, false, 2>;
     else if (variant == P2G_WARP)
-        svdj ? p2g_adj_g2p_adj_kernel<P2G_WARP, true, 2><<<n_blocks, block, 0, st>>>(a)
-        : t1 ? p2g_adj_g2p_adj_kernel<P2G_WARP, false, 3><<<n_blocks, block, 0, st>>>(a)
-             : p2g_adj_g2p_adj_kernel<P2G_WARP, false, 2><<<n_blocks, block, 0, st>>>(a);
+        k = svdj ? p2g_adj_g2p_adj_kernel<P2G_WARP, true, 2>
+            : t1 ? p2g_adj_g2p_adj_kernel<P2G_WARP, false, 3>
+                 : p2g_adj_g2p_adj_kernel<P2G_WARP, false, 2>;
     else
-        svdj ? p2g_adj_g2p_adj_kernel<P2G_VEC, true, 2><<<n_blocks, block, 0, st>>>(a)
-        : t1 ? p2g_adj_g2p_adj_kernel<P2G_VEC, false, 3><<<n_blocks, block, 0, st>>>(a)
-             : p2g_adj_g2p_adj_kernel<P2G_VEC, false, 2><<<n_blocks, block, 0, st>>>(a);
+        k = svdj ? p2g_adj_g2p_adj_kernel<P2G_VEC, true, 2>
+            : t1 ? p2g_adj_g2p_adj_kernel<P2G_VEC, false, 3>
+                 : p2g_adj_g2p_adj_kernel<P2G_VEC, false, 2>;
+    klaunch(k, n_blocks, block, st, a);
 }
 void launch_pack_state(const float* x, const float* v, const float* C, const float* F, float* st,
                        long long stride, long long n, cudaStream_t s) {

@@ -167,7 +167,11 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * "lsort" [1] (variant 4: each block of liquid particles rebuilds the
  * interleaved order over its own particles before the P2G scatter and the
  * G2P-adjoint scatter, so the lane-to-lane summation keeps working as
- * particles drift between re-sorts), "brick_scatter" /
+ * particles drift between re-sorts), "pdl" [1] (programmatic dependent
+ * launch of the substep kernels: a kernel's blocks may start while the
+ * previous kernel of the stream drains and wait in hardware for its
+ * completion before touching memory; 1 in forward rollouts, 2 also in the
+ * reverse pass, 0 never), "brick_scatter" /
  * "brick_gather" (scatter and gather forms of variant 3), "profile" [0] (1:
  * time every launch with CUDA events; totals via dstir_get_option
  * "prof_ns:<kernel>" / "prof_count:<kernel>"), "launches" (reset the launch

@@ -72,11 +72,13 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'tight': 0}, {'p2g': 4, 'reorder': 3},
             {'p2g': 1, 'reorder': 2, 'graph': 1}, {'p2g': 4, 'store_grids': 1},
             {'p2g': 4, 'store_grids': 1, 'graph': 1, 'reorder': 3}, {'p2g': 4, 'lsort': 0},
-            {'p2g': 4, 'block': 128}, {'p2g': 4, 'block': 64, 'graph': 1}]
+            {'p2g': 4, 'block': 128}, {'p2g': 4, 'block': 64, 'graph': 1}, {'p2g': 4, 'pdl': 0},
+            {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 4, 'pdl': 2, 'graph': 1}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
                'warp-tight0', 'warp-tight2', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph', 'warp-store',
-               'warp-store-graph-reorder3', 'warp-nolsort', 'warp-block128', 'warp-block64-graph']
+               'warp-store-graph-reorder3', 'warp-nolsort', 'warp-block128', 'warp-block64-graph', 'warp-nopdl',
+               'warp-fused-graph', 'warp-pdl2-graph']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
