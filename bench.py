@@ -87,6 +87,7 @@ def parse():
     ap.add_argument('--overlap', type=int, default=None, help='1: segment recompute on a second stream')
     ap.add_argument('--lsort', type=int, default=None, help='1: re-interleave each block before the warp scatters')
     ap.add_argument('--pdl', type=int, default=None, help='1: programmatic dependent launch of the substep kernels')
+    ap.add_argument('--lstage', type=int, default=None, help='1: re-interleaved P2G blocks stage their state in shared memory')
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')
@@ -280,7 +281,7 @@ def run_ours(args):
     sc = scenes[0]
     opts = {}
     keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather', 'fuse', 'fuse_adj', 'resort', 'tight',
-            'box', 'reorder', 'store_grids', 'overlap', 'lsort', 'pdl')
+            'box', 'reorder', 'store_grids', 'overlap', 'lsort', 'pdl', 'lstage')
     explicit = any(getattr(args, k) is not None for k in keys)
     if args.autotune and not explicit:
         from diffstir_gb300 import autotune
@@ -626,7 +627,7 @@ def run_ours(args):
         'gpu_launches': int(launches),
         'options': {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather',
                                                    'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder', 'store_grids', 'overlap',
-                                                   'lsort', 'pdl')},
+                                                   'lsort', 'pdl', 'lstage')},
         'clocks': clk,
         'status_flags': int(st),
     }

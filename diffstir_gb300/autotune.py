@@ -29,6 +29,7 @@ CANDIDATES = [
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 0},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1, 'lsort': 0},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1, 'pdl': 0},
+    {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1, 'lstage': 0},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1, 'pdl': 2},
     # small scenes fill few SMs with 256-particle blocks
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 128, 'gblock': 256, 'graph': 1, 'tight': 1},
@@ -54,7 +55,7 @@ def shape_key(scenes):
     rod = scenes[0].desc.rod_mode
     svd = int(any(s.desc.j_mode == 1 for s in scenes))
     name = torch.cuda.get_device_name() if torch.cuda.is_available() else 'cpu'
-    return 'v10|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
+    return 'v11|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
 
 
 def _load():

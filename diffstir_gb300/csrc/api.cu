@@ -169,6 +169,7 @@ struct DstirHandle {
     int store_grids = 0;        // option "store_grids": a recorded rollout keeps every substep's grids
     int lsort = 1;              // option "lsort": warp-aggregated scatters re-interleave each block's particles
     int pdl = 1;                // option "pdl": programmatic dependent launch, 1 forward rollouts, 2 everywhere
+    int lstage = 1;             // option "lstage": re-interleaved P2G blocks stage their state in shared memory
     bool rec_store = false;     // the recorded rollout kept its grids
     // reverse pass: the recompute of segment s-1 runs on rstream while the
     // adjoint of segment s runs on the caller's stream (double-buffered
@@ -353,6 +354,7 @@ FwdArgs fwd_args(DstirHandle* h, const float* cur, float* next, float4* pm, floa
     a.lsort = h->lsort;
     // level 1: forward rollouts only; level 2: also the reverse pass's recompute
     a.pdl = h->in_recompute ? h->pdl >= 2 : h->pdl >= 1;
+    a.lstage = h->lstage;
     return a;
 }
 
@@ -1002,7 +1004,8 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
     if (store && (rc = ensure_grid_slots(h, nsteps))) return rc;
     long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch,
                          h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0) + (vorder_on(h) ? 512 * h->reorder : 0) +
-                             (store ? (1LL << 40) : 0) + (h->lsort ? (1LL << 41) : 0) + ((long long)h->pdl << 42),
+                             (store ? (1LL << 40) : 0) + (h->lsort ? (1LL << 41) : 0) + ((long long)h->pdl << 42) +
+                             ((long long)h->lstage << 44),
                          h->block * 4096 + h->gblock};
     rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want, &h->fwd_kernels,
                          [&](cudaStream_t s2) { enqueue_forward(h, t0, nsteps, K, record != 0, store, s2); });
@@ -1253,7 +1256,7 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
     long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant * 16 + h->fuse * 2 + h->fuse_adj,
                          h->block * 4096 + h->gblock,
                          (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0) + (ovl ? 4 : 0) + (h->lsort ? 8 : 0) +
-                             16 * h->pdl,
+                             16 * h->pdl + 64 * h->lstage,
                          vorder_on(h) ? h->reorder : 0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, &h->bwd_kernels,
@@ -1326,6 +1329,10 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     }
     if (!strcmp(key, "lsort")) {
         h->lsort = value ? 1 : 0;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "lstage")) {
+        h->lstage = value ? 1 : 0;
         return DSTIR_OK;
     }
     if (!strcmp(key, "pdl")) {
@@ -1412,6 +1419,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "overlap")) *value = h->overlap;
     else if (!strcmp(key, "lsort")) *value = h->lsort;
     else if (!strcmp(key, "pdl")) *value = h->pdl;
+    else if (!strcmp(key, "lstage")) *value = h->lstage;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

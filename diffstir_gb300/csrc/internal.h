@@ -50,6 +50,9 @@ struct FwdArgs {
     int lsort = 0;
     // launch with programmatic dependent launch (see pdl_enter)
     int pdl = 0;
+    // with lsort: stage the block's state loads and F stores of P2G through
+    // shared memory
+    int lstage = 0;
 };
 
 struct AdjArgs {

@@ -41,27 +41,70 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
     bool active = p < bi.end;
     if (!active) p = bi.end - 1;  // the lane computes a copy and writes nothing
     if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
+    // re-interleaved blocks may stage their state through shared memory
+    // (lstage): thread t loads slot t (coalesced, in flight during the sort),
+    // thread s then reads the slot it processes; F[f+1] goes back the same way
+    __shared__ float pst[WARP ? NS : 1][WARP ? 256 : 1];
+    bool staged = false;
+    int slot = threadIdx.x;
     if constexpr (WARP) {
         __shared__ LocalOrderSmem lo;
         if (a.lsort && !a.order && bi.kind == KIND_LIQUID) {
-            p = bi.start + local_interleave_any(a.cur, a.stride, bi.start, (int)(bi.end - bi.start), s.inv_dx, s.n, lo);
+            const int count = (int)(bi.end - bi.start);
+            staged = a.lstage && blockDim.x <= 256;
+            if (staged && (int)threadIdx.x < count)
+#pragma unroll
+                for (int c = 0; c < NS; ++c) pst[c][threadIdx.x] = __ldg(a.cur + (long long)c * a.stride + p);
+            // local_interleave's barriers make the staged state visible
+            slot = local_interleave_any(a.cur, a.stride, bi.start, count, s.inv_dx, s.n, lo);
+            p = bi.start + slot;
             active = p < bi.end;
-            if (!active) p = bi.end - 1;
+            if (!active) {
+                p = bi.end - 1;
+                slot = count - 1;
+            }
         }
     }
     float x[3], v[3], C[9];
-    load3(a.cur, a.stride, OX, p, x);
-    load3(a.cur, a.stride, OV, p, v);
-    load9(a.cur, a.stride, OC, p, C);
+    if (staged) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            x[c] = pst[OX + c][slot];
+            v[c] = pst[OV + c][slot];
+        }
+#pragma unroll
+        for (int i = 0; i < 9; ++i) C[i] = pst[OC + i][slot];
+    } else {
+        load3(a.cur, a.stride, OX, p, x);
+        load3(a.cur, a.stride, OV, p, v);
+        load9(a.cur, a.stride, OC, p, C);
+    }
     float m, vv[3], A[9];
     if (bi.kind == KIND_LIQUID) {
         float F[9], prm[4];
-        load9(a.cur, a.stride, OF, p, F);
+        if (staged) {
+#pragma unroll
+            for (int i = 0; i < 9; ++i) F[i] = pst[OF + i][slot];
+        } else {
+            load9(a.cur, a.stride, OF, p, F);
+        }
 #pragma unroll
         for (int i = 0; i < 4; ++i) prm[i] = __ldg(a.params + bi.scene * 4 + i);
         LiquidP2G q;
         liquid_p2g<SVDJ>(s, __ldg(a.models + bi.scene), prm, v, C, F, q);
-        if (active) store9(a.next, a.stride, OF, p, q.Ft);  // F[f+1] = F_tmp (:153)
+        if (staged) {  // block-uniform
+            __syncthreads();  // every thread has read its staged F
+            if (active)
+#pragma unroll
+                for (int i = 0; i < 9; ++i) pst[OF + i][slot] = q.Ft[i];
+            __syncthreads();
+            const long long t = bi.start + threadIdx.x;
+            if (t < bi.end)
+#pragma unroll
+                for (int i = 0; i < 9; ++i) a.next[(long long)(OF + i) * a.stride + t] = pst[OF + i][threadIdx.x];
+        } else if (active) {
+            store9(a.next, a.stride, OF, p, q.Ft);  // F[f+1] = F_tmp (:153)
+        }
         m = s.m_liq;
 #pragma unroll
         for (int i = 0; i < 9; ++i) A[i] = q.A[i];

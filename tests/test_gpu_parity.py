@@ -73,12 +73,13 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 1, 'reorder': 2, 'graph': 1}, {'p2g': 4, 'store_grids': 1},
             {'p2g': 4, 'store_grids': 1, 'graph': 1, 'reorder': 3}, {'p2g': 4, 'lsort': 0},
             {'p2g': 4, 'block': 128}, {'p2g': 4, 'block': 64, 'graph': 1}, {'p2g': 4, 'pdl': 0},
-            {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 4, 'pdl': 2, 'graph': 1}]
+            {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 4, 'pdl': 2, 'graph': 1},
+            {'p2g': 4, 'lstage': 0}, {'p2g': 4, 'graph': 1, 'block': 128, 'tight': 2}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
                'warp-tight0', 'warp-tight2', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph', 'warp-store',
                'warp-store-graph-reorder3', 'warp-nolsort', 'warp-block128', 'warp-block64-graph', 'warp-nopdl',
-               'warp-fused-graph', 'warp-pdl2-graph']
+               'warp-fused-graph', 'warp-pdl2-graph', 'warp-nostage', 'warp-graph-block128-tight2']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
@@ -223,7 +224,8 @@ def test_resort_matches_fixed_order(opts):
 
 
 @pytest.mark.parametrize('block', [256, 128, 64])
-def test_local_interleave_matches_block_order(block):
+@pytest.mark.parametrize('lstage', [0, 1])
+def test_local_interleave_matches_block_order(block, lstage):
     """Rebuilding the interleaved order inside each block before the warp
     scatters (option lsort) only changes which lane handles which particle:
     forces, final state, parameter gradient and the adjoint of the step-0
@@ -236,7 +238,7 @@ def test_local_interleave_matches_block_order(block):
     wts = torch.as_tensor(np.random.default_rng(6).normal(size=(2, T, 3)), dtype=torch.float32, device='cuda')
     out = {}
     for ls in (0, 1):
-        sim = Simulator(scenes, max_steps=T, options={'p2g': 4, 'lsort': ls, 'block': block})
+        sim = Simulator(scenes, max_steps=T, options={'p2g': 4, 'lsort': ls, 'block': block, 'lstage': lstage})
         assert sim.get_option('lsort') == ls
         sim.reset()
         f = sim.forward(T, ckpt_every=K, record=True).cpu().numpy()
