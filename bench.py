@@ -87,7 +87,7 @@ def parse():
     ap.add_argument('--overlap', type=int, default=None, help='1: segment recompute on a second stream')
     ap.add_argument('--lsort', type=int, default=None, help='1: re-interleave each block before the warp scatters')
     ap.add_argument('--pdl', type=int, default=None, help='1: programmatic dependent launch of the substep kernels')
-    ap.add_argument('--lstage', type=int, default=None, help='1: re-interleaved P2G blocks stage their state in shared memory')
+    ap.add_argument('--lstage', type=int, default=None, help='re-interleaved blocks stage their state in shared memory (bits: P2G, G2P adjoint)')
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')

@@ -169,7 +169,7 @@ struct DstirHandle {
     int store_grids = 0;        // option "store_grids": a recorded rollout keeps every substep's grids
     int lsort = 1;              // option "lsort": warp-aggregated scatters re-interleave each block's particles
     int pdl = 1;                // option "pdl": programmatic dependent launch, 1 forward rollouts, 2 everywhere
-    int lstage = 1;             // option "lstage": re-interleaved P2G blocks stage their state in shared memory
+    int lstage = 3;             // option "lstage": re-interleaved blocks stage their state in shared memory (bit 0 P2G, bit 1 G2P adjoint)
     bool rec_store = false;     // the recorded rollout kept its grids
     // reverse pass: the recompute of segment s-1 runs on rstream while the
     // adjoint of segment s runs on the caller's stream (double-buffered
@@ -1146,6 +1146,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.order = h->rec_store ? nullptr : vorder_slot(h, k, true);
             a.lsort = h->lsort;
             a.pdl = h->pdl >= 2;
+            a.lstage = h->lstage;
             return a;
         };
         if (!fused_adj(h)) {
@@ -1332,7 +1333,8 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         return DSTIR_OK;
     }
     if (!strcmp(key, "lstage")) {
-        h->lstage = value ? 1 : 0;
+        if (value < 0 || value > 3) return fail(h, DSTIR_EINVAL, "lstage must be 0..3");
+        h->lstage = (int)value;
         return DSTIR_OK;
     }
     if (!strcmp(key, "pdl")) {

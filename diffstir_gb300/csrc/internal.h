@@ -87,6 +87,7 @@ struct AdjArgs {
     const int* order = nullptr;      // processing order (see FwdArgs::order) or NULL
     int lsort = 0;                   // warp-aggregated G2P adjoint: see FwdArgs::lsort
     int pdl = 0;                     // see FwdArgs::pdl
+    int lstage = 0;                  // G2P adjoint: see FwdArgs::lstage
 };
 
 // Counting sort of the particles of one substep by stencil-base cell.

@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
         __shared__ LocalOrderSmem lo;
         if (a.lsort && !a.order && bi.kind == KIND_LIQUID) {
             const int count = (int)(bi.end - bi.start);
-            staged = a.lstage && blockDim.x <= 256;
+            staged = (a.lstage & 1) && blockDim.x <= 256;
             if (staged && (int)threadIdx.x < count)
 #pragma unroll
                 for (int c = 0; c < NS; ++c) pst[c][threadIdx.x] = __ldg(a.cur + (long long)c * a.stride + p);
@@ -609,22 +609,57 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
     if (!WARP && !active) return;
     if (!active) p = bi.end - 1;  // WARP: the lane computes a copy and scatters nothing
     if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
+    // re-interleaved blocks may stage their inputs through shared memory
+    // (lstage, as in P2G): row c < 3 holds x of the state, row 3 + c
+    // component c of the next state's adjoint; rows 0-2 later carry the
+    // position adjoint back
+    __shared__ float ast[WARP ? 18 : 1][WARP ? 256 : 1];
+    bool staged = false;
+    int slot = threadIdx.x;
     if constexpr (WARP) {
         __shared__ LocalOrderSmem lo;
         if (a.lsort && !a.order && bi.kind == KIND_LIQUID) {
-            p = bi.start + local_interleave_any(a.cur, a.stride, bi.start, (int)(bi.end - bi.start), s.inv_dx, s.n, lo);
+            const int count = (int)(bi.end - bi.start);
+            staged = (a.lstage & 2) && blockDim.x <= 256;
+            if (staged && (int)threadIdx.x < count) {
+#pragma unroll
+                for (int c = 0; c < 3; ++c) ast[c][threadIdx.x] = __ldg(a.cur + (long long)(OX + c) * a.stride + p);
+#pragma unroll
+                for (int c = 0; c < 15; ++c) ast[3 + c][threadIdx.x] = a.adj_next[(long long)c * a.stride + p];
+            }
+            // local_interleave's barriers make the staged inputs visible
+            slot = local_interleave_any(a.cur, a.stride, bi.start, count, s.inv_dx, s.n, lo);
+            p = bi.start + slot;
             active = p < bi.end;
-            if (!active) p = bi.end - 1;
+            if (!active) {
+                p = bi.end - 1;
+                slot = count - 1;
+            }
         }
     }
     float x[3];
-    load3(a.cur, a.stride, OX, p, x);
     float xb[3] = {0.f, 0.f, 0.f}, vnb[3], Cb[9];
-    load9(a.adj_next, a.stride, OC, p, Cb);
+    if (staged) {
+#pragma unroll
+        for (int c = 0; c < 3; ++c) x[c] = ast[OX + c][slot];
+#pragma unroll
+        for (int i = 0; i < 9; ++i) Cb[i] = ast[3 + OC + i][slot];
+    } else {
+        load3(a.cur, a.stride, OX, p, x);
+        load9(a.adj_next, a.stride, OC, p, Cb);
+    }
     if (bi.kind == KIND_LIQUID) {
         float ax[3], av[3];
-        load3(a.adj_next, a.stride, OX, p, ax);
-        load3(a.adj_next, a.stride, OV, p, av);
+        if (staged) {
+#pragma unroll
+            for (int c = 0; c < 3; ++c) {
+                ax[c] = ast[3 + OX + c][slot];
+                av[c] = ast[3 + OV + c][slot];
+            }
+        } else {
+            load3(a.adj_next, a.stride, OX, p, ax);
+            load3(a.adj_next, a.stride, OV, p, av);
+        }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
             vnb[c] = av[c] + s.dt * ax[c];  // x[f+1] = x[f] + dt*v[f+1] (:247)
@@ -705,7 +740,19 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
             for (int b = 0; b < 3; ++b)
                 xb[b] += s.inv_dx * (fxb[b] - (Cc[0 * 3 + b] * U[0] + Cc[1 * 3 + b] * U[1] + Cc[2 * 3 + b] * U[2]));
     }
-    if (bi.kind == KIND_LIQUID && active) store3(a.adj_cur, a.stride, OX, p, xb);
+    if (staged) {  // block-uniform
+        __syncthreads();  // every thread has read its staged inputs
+        if (active)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) ast[c][slot] = xb[c];
+        __syncthreads();
+        const long long t = bi.start + threadIdx.x;
+        if (t < bi.end)
+#pragma unroll
+            for (int c = 0; c < 3; ++c) a.adj_cur[(long long)(OX + c) * a.stride + t] = ast[c][threadIdx.x];
+    } else if (bi.kind == KIND_LIQUID && active) {
+        store3(a.adj_cur, a.stride, OX, p, xb);
+    }
 }
 
 __global__ void __launch_bounds__(1024) grid_adj_kernel(AdjArgs a) {

@@ -167,9 +167,10 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * "lsort" [1] (variant 4: each block of liquid particles rebuilds the
  * interleaved order over its own particles before the P2G scatter and the
  * G2P-adjoint scatter, so the lane-to-lane summation keeps working as
- * particles drift between re-sorts), "lstage" [1] (with "lsort": the
- * block's state is loaded coalesced into shared memory while the block
- * sorts, and F of the next state goes back the same way), "pdl" [1]
+ * particles drift between re-sorts), "lstage" [3] (with "lsort": the
+ * block's inputs are loaded coalesced into shared memory while the block
+ * sorts, and its outputs go back the same way; bit 0 P2G, bit 1 the G2P
+ * adjoint), "pdl" [1]
  * (programmatic dependent
  * launch of the substep kernels: a kernel's blocks may start while the
  * previous kernel of the stream drains and wait in hardware for its
