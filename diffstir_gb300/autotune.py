@@ -24,6 +24,7 @@ CANDIDATES = [
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 256, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 2},
+    {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 256, 'graph': 1, 'tight': 2},
     {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 1, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 0},
