@@ -238,6 +238,8 @@ def main(argv=None):
     ap.add_argument('--frames-per-clip', type=int, default=0,
                     help='> 0: clip-wise identification with the state carried from clip to clip')
     ap.add_argument('--carry', default='x', choices=['x', 'full'])
+    ap.add_argument('--autotune', type=int, default=1,
+                    help='1: launch options of the batched handle from the autotuner (cached)')
     args = ap.parse_args(argv)
     cfg = S.CONFIGS[args.config]
     T = args.substeps or cfg['n_steps']
@@ -266,8 +268,12 @@ def main(argv=None):
                          for c in clips]}
         print(json.dumps(out), flush=True)
         return out
+    opts = None
+    if args.autotune:
+        from . import autotune
+        opts = autotune.autotune([copy.copy(sc) for _ in range(R)])
     res = adam_identify(sc, target, restarts=R, iters=args.iters, lr=args.lr, ckpt_every=args.ckpt or cfg['ckpt'],
-                        free=free, bounds=bounds, seed=args.seed + 1)
+                        free=free, bounds=bounds, seed=args.seed + 1, options=opts)
     res['sim'].close()
     plain = None
     if args.plain_iters > 0:
@@ -280,7 +286,7 @@ def main(argv=None):
     rel = {name: float(abs(best[i] - truth[i]) / max(abs(truth[i]), 1e-12)) for name, i in
            (('K', 0), ('tau_y', 1), ('n', 2)) if i in free}
     out = {'config': args.config, 'particles': sc.n_particles, 'substeps': T, 'restarts': R, 'iters': args.iters,
-           'truth': truth.tolist(), 'best': best.tolist(), 'rel_err': rel,
+           'options': opts, 'truth': truth.tolist(), 'best': best.tolist(), 'rel_err': rel,
            'best_loss': float(res['best_loss'].min()), 'initial_loss_min': float(res['history'][0].min()),
            'wall_s': res['wall_s'], 'grad_evals': res['grad_evals'],
            'grad_evals_per_s': res['grad_evals_per_s'], 'plain_grad_evals_per_s': plain,
