@@ -109,7 +109,7 @@ struct DstirHandle {
     std::vector<DstirSceneDesc> desc;
     std::vector<SceneDev> sc_h;
     long long N = 0, stride = 0, G = 0;
-    int block = 256, gblock = 1024, p2g_variant = P2G_WARP, use_graph = 0;
+    int block = 256, gblock = 1024, p2g_variant = P2G_WARP, use_graph = 1;
     int brick_gather = 1;   // with P2G_BRICK: G2P and the P2G adjoint also gather from brick tiles
     int brick_scatter = 1;  // with P2G_BRICK: 0 shared atomics, 1 shared red, 2 direct global atomics
     int fuse = 0;           // per-particle variants: G2P(f) and P2G(f+1) in one kernel (measured 4% slower at 64^3)

@@ -147,7 +147,7 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * contributions to shared stencil nodes by warp shuffles; 2, 3 and 4 also
  * select the matching G2P-adjoint scatter; variant 2 also sets gblock to 256),
  * "block" [256] (threads per particle block: 64, 128 or 256), "gblock" [1024]
- * (threads per grid block: 64 to 1024, at most 256 with variant 2), "graph" [0] (1:
+ * (threads per grid block: 64 to 1024, at most 256 with variant 2), "graph" [1] (1:
  * replay each rollout and each reverse pass as a cached CUDA graph), "fuse" /
  * "fuse_adj" [0] (1: G2P of substep f fused with P2G of f+1 / P2G adjoint of
  * f fused with the G2P adjoint of f-1), "resort" [1] (re-sort the particle

@@ -74,12 +74,12 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 4, 'store_grids': 1, 'graph': 1, 'reorder': 3}, {'p2g': 4, 'lsort': 0},
             {'p2g': 4, 'block': 128}, {'p2g': 4, 'block': 64, 'graph': 1}, {'p2g': 4, 'pdl': 0},
             {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 4, 'pdl': 2, 'graph': 1},
-            {'p2g': 4, 'lstage': 0}, {'p2g': 4, 'graph': 1, 'block': 128, 'tight': 2}]
+            {'p2g': 4, 'lstage': 0}, {'p2g': 4, 'graph': 1, 'block': 128, 'tight': 2}, {'p2g': 4, 'graph': 0}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
                'warp-tight0', 'warp-tight2', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph', 'warp-store',
                'warp-store-graph-reorder3', 'warp-nolsort', 'warp-block128', 'warp-block64-graph', 'warp-nopdl',
-               'warp-fused-graph', 'warp-pdl2-graph', 'warp-nostage', 'warp-graph-block128-tight2']
+               'warp-fused-graph', 'warp-pdl2-graph', 'warp-nostage', 'warp-graph-block128-tight2', 'warp-eager']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
@@ -402,7 +402,7 @@ def test_graph_replay_matches_eager_and_is_reusable():
     T = 18
     sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=7))
     wts = torch.as_tensor(np.random.default_rng(8).normal(size=(1, T, 3)), dtype=torch.float32, device='cuda')
-    eager = Simulator(sc, max_steps=T, options={'p2g': 2})
+    eager = Simulator(sc, max_steps=T, options={'p2g': 2, 'graph': 0})
     graph = Simulator(sc, max_steps=T, options={'p2g': 2, 'graph': 1})
     fe = eager.forward(T, ckpt_every=5, record=True)
     ge = eager.backward(wts)
