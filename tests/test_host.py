@@ -1,12 +1,17 @@
 """Host-side logic without a GPU: the reference-scene builder against the
 scene the reference's own code built (golden fixtures), the compat module's
-API surface, the reference's step rule, and the synthetic scene generators."""
+API surface, the reference's step rule, the synthetic scene generators, and the launch
+options the autotuner and the bench pass against the header's list."""
+
+import os
 
 import numpy as np
 import pytest
 
 import golden_util as gu
 from diffstir_gb300 import scene as S
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 
 @pytest.mark.parametrize('name', ['ref_f64_g32', 'ref_f64_g71'])
@@ -98,3 +103,25 @@ def test_product_fails_loudly_without_gpu():
     from diffstir_gb300.simulator import Simulator
     with pytest.raises(RuntimeError):
         Simulator(S.small_synthetic_scene(n_steps=2))
+
+
+def _documented_options():
+    import re
+    src = open(os.path.join(ROOT, 'include', 'diffstir.h')).read()
+    i, j = src.index('/* Tuning knobs'), src.index('int dstir_set_option')
+    return set(re.findall(r'"([a-z_0-9]+)"', src[i:j]))
+
+
+def test_autotune_candidates_use_documented_options():
+    from diffstir_gb300 import autotune
+    keys = _documented_options()
+    for cand in autotune.CANDIDATES:
+        assert set(cand) <= keys, set(cand) - keys
+
+
+def test_bench_option_flags_are_documented_options():
+    import re
+    src = open(os.path.join(ROOT, 'bench.py')).read()
+    m = re.search(r"keys = \(([^)]*)\)", src)
+    names = set(re.findall(r"'([a-z_0-9]+)'", m.group(1)))
+    assert names and names <= _documented_options(), names - _documented_options()
