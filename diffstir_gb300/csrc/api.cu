@@ -163,7 +163,7 @@ struct DstirHandle {
     // periodic re-sort of the particle order (per-particle variants): every K
     // substeps of a rollout, at the checkpoint boundaries of a recorded one
     int resort = 1;             // option "resort": 0 never
-    int tight = 1;              // option "tight": register-cap level of the particle kernels (0, 1, 2)
+    int tight = 2;              // option "tight": register-cap level of the particle kernels (0, 1, 2)
     int use_box = 1;            // option "box": the grid kernels skip nodes outside the occupied box
     int reorder = 0;            // option "reorder": processing order rebuilt every this many substeps (0: never)
     int store_grids = 0;        // option "store_grids": a recorded rollout keeps every substep's grids

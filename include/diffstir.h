@@ -152,7 +152,7 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * "fuse_adj" [0] (1: G2P of substep f fused with P2G of f+1 / P2G adjoint of
  * f fused with the G2P adjoint of f-1), "resort" [1] (re-sort the particle
  * order every ckpt_every substeps of a rollout; states and state adjoints
- * still cross the ABI in the order given to dstir_set_state), "tight" [1]
+ * still cross the ABI in the order given to dstir_set_state), "tight" [2]
  * (register-cap level of the particle kernels, 0..2), "box" [1] (P2G records
  * each scene's occupied node box and the grid update and its adjoint skip the
  * nodes outside it; per-particle variants only), "reorder" [0] (rebuild the

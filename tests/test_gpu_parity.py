@@ -68,7 +68,7 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 0, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 2}, {'p2g': 3},
             {'p2g': 3, 'brick_scatter': 0}, {'p2g': 3, 'brick_scatter': 2}, {'p2g': 3, 'brick_gather': 0},
             {'p2g': 3, 'graph': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 4, 'resort': 0},
-            {'p2g': 4, 'graph': 1}, {'p2g': 4, 'tight': 0}, {'p2g': 4, 'tight': 2},
+            {'p2g': 4, 'graph': 1}, {'p2g': 4, 'tight': 0}, {'p2g': 4, 'tight': 1},
             {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'tight': 0}, {'p2g': 4, 'reorder': 3},
             {'p2g': 1, 'reorder': 2, 'graph': 1}, {'p2g': 4, 'store_grids': 1},
             {'p2g': 4, 'store_grids': 1, 'graph': 1, 'reorder': 3}, {'p2g': 4, 'lsort': 0},
@@ -77,7 +77,7 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 4, 'lstage': 0}, {'p2g': 4, 'graph': 1, 'block': 128, 'tight': 2}, {'p2g': 4, 'graph': 0}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
-               'warp-tight0', 'warp-tight2', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph', 'warp-store',
+               'warp-tight0', 'warp-tight1', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph', 'warp-store',
                'warp-store-graph-reorder3', 'warp-nolsort', 'warp-block128', 'warp-block64-graph', 'warp-nopdl',
                'warp-fused-graph', 'warp-pdl2-graph', 'warp-nostage', 'warp-graph-block128-tight2', 'warp-eager']
 
