@@ -88,3 +88,34 @@ def test_block_reinterleave_cuts_red_sectors_after_drift():
     assert blk_drift > 1.1 * blk_fresh, (blk_fresh, blk_drift)
     assert ri_drift < 0.85 * blk_drift, (ri_drift, blk_drift)
     assert ri_fresh <= 1.01 * blk_fresh, (ri_fresh, blk_fresh)
+
+
+def test_simulator_initial_order_is_the_interleaved_order():
+    """The order the Simulator hands the handle (simulator.interleaved_order)
+    is the (row, rank, k) order of the re-sort, per scene and particle kind:
+    a permutation inside each range, with (i, j, rank, k) non-decreasing."""
+    from diffstir_gb300.simulator import interleaved_order
+    scenes = [S.small_synthetic_scene(n_grid=16, ppc=4, n_steps=4, seed=21),
+              S.small_synthetic_scene(n_grid=20, ppc=8, n_steps=4, seed=22)]
+    x0 = np.concatenate([sc.x0() for sc in scenes], 0)
+    perm = interleaved_order(scenes, x0)
+    off = 0
+    for sc in scenes:
+        n = sc.desc.n_grid
+        for cnt in (sc.desc.n_liquid, sc.desc.n_rod, sc.desc.n_container):
+            seg = perm[off:off + cnt]
+            assert np.array_equal(np.sort(seg), np.arange(off, off + cnt))
+            if cnt:
+                keys = base_keys(x0[seg], n)
+                # rank of each particle inside its cell, in the order given
+                o = np.argsort(keys, kind='stable')
+                ks = keys[o]
+                rank = np.empty(cnt, np.int64)
+                rank[o] = np.arange(cnt) - np.searchsorted(ks, ks, side='left')
+                tup = np.stack([keys // n, rank, keys % n], 1)
+                assert np.all(np.diff(tup[:, 0]) >= 0)
+                same_row = np.diff(tup[:, 0]) == 0
+                step = np.diff(tup[:, 1:], axis=0)
+                assert np.all((step[same_row, 0] > 0) | ((step[same_row, 0] == 0) & (step[same_row, 1] > 0)))
+                assert red_sectors(keys, n) == red_sectors(keys[interleave(keys, n)], n)
+            off += cnt
