@@ -2,7 +2,8 @@
 optimises in normalised coordinates inside the parameter box, keeps the best
 parameters of every restart, and starts restart 0 from init_params;
 clip_identify fits clip windows in order and carries the state (positions, or
-the full state) from one clip's best-parameter rollout into the next.  The
+the full state) from one clip's best-parameter rollout into the next;
+export_profiles writes one x and one z profile per scene.  The
 simulator is replaced by a differentiable stand-in whose force profile is
 smooth in (K, n), so the driver itself is what is tested."""
 
@@ -136,3 +137,20 @@ def test_clip_identify_windows_and_state_carry(monkeypatch, carry):
         assert inits[k][2] == pytest.approx(y0 + 0.001 * fpc * clip, abs=1e-5)
         assert inits[k][3] == (carry == 'full') and inits[k][4] == (carry == 'full')
     assert inits[0][1] == 2 and inits[1][1] == 1  # tiled over the restarts, then one scene
+
+
+def test_export_profiles_writes_x_and_z_per_scene(tmp_path):
+    from diffstir_gb300 import export
+
+    class Sim:
+        def forward(self, nsteps):
+            f = torch.arange(2 * nsteps * 3, dtype=torch.float32).reshape(2, nsteps, 3)
+            return f
+
+    f = export.export_profiles(Sim(), 5, str(tmp_path), prefix='r_')
+    for b in range(2):
+        fx = np.load(str(tmp_path / ('r_force_profile_x_%d.npy' % b)))
+        fz = np.load(str(tmp_path / ('r_force_profile_z_%d.npy' % b)))
+        assert fx.dtype == np.float32 and fx.shape == (5,)
+        np.testing.assert_array_equal(fx, f[b, :, 0])
+        np.testing.assert_array_equal(fz, f[b, :, 2])
