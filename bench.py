@@ -180,6 +180,18 @@ def ncu_traffic(kernel, workload):
     return ncu_value('traffic_bytes_per_launch', kernel, workload)
 
 
+def fp32_peak():
+    """FP32 FMA flop/s this GPU sustains (dstir_measure_fp32_rate), or None."""
+    import ctypes
+    import torch
+    from diffstir_gb300 import _lib
+    rate = ctypes.c_double(0.0)
+    torch.cuda.synchronize()
+    rc = _lib.lib().dstir_measure_fp32_rate(20000, ctypes.byref(rate),
+                                            ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    return rate.value if rc == 0 else None
+
+
 def red_peak(G):
     """Vector-RED sectors/s this GPU retires on a grid of G nodes
     (dstir_measure_red_rate), or None."""
@@ -592,6 +604,14 @@ def run_ours(args):
             ach = sec / (t_ms / 1e3 / c) if sec else None
             red_roof[k] = {'sectors_per_launch': sec, 'avg_launch_us': t_ms / c * 1e3, 'achieved': ach,
                            'frac': ach / peak_red if (ach and peak_red) else None}
+    # FP32 side of the roofline: the FMA-pipe issue fraction of each particle
+    # kernel over its launch (committed ncu summary), beside the FP32 FMA rate
+    # measured on this GPU
+    fp32_roof = {'peak': fp32_peak(), 'unit': 'flop/s', 'peak_kind': 'measured: independent FMA chains',
+                 'fma_pipe_frac': {k: ncu_value('fp32_pipe_frac', k, args.config)
+                                   for k in ('p2g', 'grid', 'g2p', 'g2p_adj', 'grid_adj', 'p2g_adj')},
+                 'what': 'share of the FMA pipe issue peak used while the kernel runs '
+                         '(ncu sm__inst_executed_pipe_fma, of peak sustained active)'}
     # whole-step algorithmic bytes: forward 192 N + 56 G, adjoint 480 N + 112 G per substep
     step_bytes = T * ((192 + 480) * N + (56 + 112) * G)
     kernel_share = {k: round(prof[k][0] / max(sum(v[0] for v in prof.values()), 1e-9), 4) for k in KERNELS}
@@ -622,6 +642,7 @@ def run_ours(args):
         'roofline': roof,
         'kernel_time_share': kernel_share,
         'roofline_l2_red': red_roof,
+        'roofline_fp32': fp32_roof,
         'cpu_baseline': cpu,
         'e2e': e2e,
         'gpu_launches': int(launches),

@@ -70,6 +70,7 @@ PROTOTYPES = {
     'dstir_svd3_backward': (C.c_int, [P, P, P, P, P, P, P, C.c_int64, P]),
     'dstir_substep_static': (C.c_int, [C.POINTER(DstirSceneDesc), P, P, P, P, P, P]),
     'dstir_measure_red_rate': (C.c_int, [C.c_int64, C.c_int32, C.POINTER(C.c_double), P]),
+    'dstir_measure_fp32_rate': (C.c_int, [C.c_int32, C.POINTER(C.c_double), P]),
 }
 
 

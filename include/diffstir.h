@@ -219,6 +219,10 @@ int dstir_substep_static(const DstirSceneDesc* scene, const float* params, const
  * warp-aggregated P2G and G2P-adjoint scatters.  Allocates and frees its own
  * grid; synchronises the stream.  sectors_per_s: host pointer. */
 int dstir_measure_red_rate(int64_t n_nodes, int32_t reps, double* sectors_per_s, void* stream);
+/* Diagnostics: FP32 FMA throughput of this GPU (flop/s, an FMA counting two),
+ * from eight independent FMA chains per thread over 8 blocks of 256 threads
+ * per SM.  Synchronises the stream.  flops_per_s: host pointer. */
+int dstir_measure_fp32_rate(int32_t iters, double* flops_per_s, void* stream);
 
 #ifdef __cplusplus
 }

@@ -43,3 +43,10 @@ def test_red_rate_probe_rejects_bad_arguments_before_any_cuda_call():
     assert lib.dstir_measure_red_rate(16, 8, ctypes.byref(rate), None) == -1
     assert lib.dstir_measure_red_rate(1 << 18, 0, ctypes.byref(rate), None) == -1
     assert lib.dstir_measure_red_rate(1 << 18, 8, None, None) == -1
+
+
+def test_fp32_rate_probe_rejects_bad_arguments_before_any_cuda_call():
+    lib = _abi.bind(ctypes.CDLL(build()))
+    rate = ctypes.c_double(0.0)
+    assert lib.dstir_measure_fp32_rate(0, ctypes.byref(rate), None) == -1
+    assert lib.dstir_measure_fp32_rate(16, None, None) == -1

@@ -165,3 +165,15 @@ def test_red_rate_probe_measures_a_positive_rate():
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     assert _lib.lib().dstir_measure_red_rate(1 << 18, 64, ctypes.byref(rate), s) == 0
     assert 1e9 < rate.value < 1e13, rate.value
+
+
+@pytest.mark.gpu
+def test_fp32_rate_probe_measures_a_plausible_rate():
+    """The FP32 FMA probe behind the FP32 side of the roofline reports a rate
+    between 1 and 1000 TFLOP/s."""
+    import ctypes
+    from diffstir_gb300 import _lib
+    rate = ctypes.c_double(0.0)
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    assert _lib.lib().dstir_measure_fp32_rate(2000, ctypes.byref(rate), s) == 0
+    assert 1e12 < rate.value < 1e15, rate.value
