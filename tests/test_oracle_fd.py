@@ -227,3 +227,37 @@ def test_sticky_top_is_what_separates_adjoint_and_differences():
         gaps[variant] = max(rel)
     assert gaps[None] > 1e-3
     assert gaps['continuous_top'] < 1e-5
+
+
+@pytest.mark.parametrize('T', [1, 3])
+def test_state_to_state_adjoint_dot_product(T):
+    """Dot-product test of the state-to-state adjoint of whole substeps (P2G,
+    grid update and G2P with their adjoints): with a random adjoint W of the
+    final state and random weights w of the forces, <W, dS_T/dS_0 u> +
+    <w, dF/dS_0 u> by central differences along a random full-state
+    direction u equals <dL/dS_0, u> from the reverse pass seeded with W."""
+    sc = S.small_synthetic_scene(n_grid=12, ppc=2, n_steps=T, seed=9, dt=5e-4)
+    rng = np.random.default_rng(17)
+    x0 = sc.x0()
+    n = x0.shape[0]
+    v0 = rng.normal(scale=0.05, size=(n, 3))
+    C0 = rng.normal(scale=0.2, size=(n, 9))
+    F0 = np.tile(np.eye(3).reshape(1, 9), (n, 1)) + rng.normal(scale=0.01, size=(n, 9))
+    wts = rng.normal(size=(T, 3))
+    W = rng.normal(size=(n, 24))
+    _, _, ds, st = oracle.grad_seeded(sc.desc, sc.params, sc.trajectory, T, x0, wts, W, v0, C0, F0)
+    assert st == 0
+    u = rng.normal(size=(n, 24))
+    u[:, :3] *= 1e-2
+    h = 1e-6
+
+    def proj(sign):
+        f, last, _ = oracle.rollout_last(sc.desc, sc.params, sc.trajectory, T, x0 + sign * h * u[:, :3],
+                                         v0 + sign * h * u[:, 3:6], C0 + sign * h * u[:, 6:15],
+                                         F0 + sign * h * u[:, 15:])
+        return float((wts * f).sum()) + float((W * last).sum())
+
+    jvp = (proj(1) - proj(-1)) / (2 * h)
+    vjp = float((ds * u).sum())
+    assert abs(jvp) > 0
+    assert abs(vjp - jvp) <= 1e-6 * abs(jvp), (vjp, jvp)
