@@ -5,7 +5,9 @@ src/force_calculation_and_animation_module.py, main.py) do
 ``from src.simulator.simulation_functions import *`` and then drive module-level
 Taichi kernels and fields.  This module exposes the same names with the same
 meaning, backed by the GB300 simulator, so those callers run unchanged when
-that import is redirected here (INTEGRATION.md shows the one-line shim)::
+that import is redirected here, for instance by
+``sys.modules['src.simulator.simulation_functions'] = diffstir_gb300.compat``
+before the caller's own import runs::
 
     initialize_objects(), initialize_ti_field(), forward(f), backward(f),
     compute_loss(), ti.ad.Tape(loss=loss)

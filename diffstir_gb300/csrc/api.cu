@@ -10,6 +10,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -489,6 +490,17 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
     if (!out) return DSTIR_EINVAL;
     *out = nullptr;
     if (!scenes || batch <= 0 || max_steps <= 0) return DSTIR_EINVAL;
+    // grid-node and bin keys are 32-bit in the re-sort and the binned
+    // variants: the batch's nodes must fit in INT_MAX (checked before anything
+    // is built or allocated)
+    {
+        long long g_all = 0;
+        for (int s = 0; s < batch; ++s) {
+            const long long n = scenes[s].n_grid;
+            if (n >= 4 && n <= 1024) g_all += n * n * n;
+            if (g_all > (long long)INT_MAX) return DSTIR_ERANGE;
+        }
+    }
     DstirHandle* h = new (std::nothrow) DstirHandle();
     if (!h) return DSTIR_ENOMEM;
     h->B = batch;

@@ -10,18 +10,20 @@
 // one file-scope static device array, kScratchBytes (about 8.3 MB) in size.
 // Every GPU that loads the library holds that array until the process exits.
 //
-// Limits: at most kMaxNodes grid nodes (n_grid <= 64) and kMaxParticles
-// particles; larger scenes are rejected with DSTIR_ERANGE.
+// Limits: n_grid <= kMaxAxis (64, so at most kMaxNodes grid nodes) and at most
+// kMaxParticles particles; larger scenes are rejected with DSTIR_ERANGE before
+// anything is queued.
 //
 // The array is shared by every call: each call clears what must start at zero
 // (the P2G grid and the reduction counters) before use, and two calls whose
 // work overlaps on the GPU (different streams, or different host threads)
 // race on it.  Serialise them.
 //
-// The array's name is a host-side stand-in, not a device address.  The first
-// call on each device, with that device current, asks the runtime for the
-// array's device address (cudaGetSymbolAddress) and keeps it; make that first
-// call before any stream capture, since the lookup may initialise the module.
+// The array's name is a host-side stand-in, not a device address.  Every call,
+// with the caller's device current, asks the runtime for the array's device
+// address (cudaGetSymbolAddress: no allocation), so the address stays right
+// across a device reset.  The first call on a device may load the module;
+// make it before any stream capture.
 #include <cuda_runtime.h>
 
 #include <cstring>
@@ -32,7 +34,8 @@
 namespace dstir {
 namespace {
 
-constexpr long long kMaxNodes = 64LL * 64 * 64;
+constexpr int kMaxAxis = 64;
+constexpr long long kMaxNodes = (long long)kMaxAxis * kMaxAxis * kMaxAxis;
 constexpr long long kMaxParticles = 1LL << 20;
 constexpr int kBlock = 256;
 constexpr long long kMaxPBlocks = kMaxParticles / kBlock + 3;   // + one partial block per particle kind
@@ -51,20 +54,12 @@ constexpr size_t kScratchBytes = align256(kOffMisc + 16 * sizeof(unsigned));
 
 static __device__ __align__(256) unsigned char g_static_scratch[kScratchBytes];
 
-constexpr int kMaxDevices = 64;
-unsigned char* g_scratch_ptr[kMaxDevices] = {nullptr};
-
+// Device address of the scratch array on the current device.
 int scratch_for_current_device(unsigned char** out) {
-    int dev = 0;
-    if (cudaGetDevice(&dev) != cudaSuccess) return DSTIR_ECUDA;
-    if (dev < 0 || dev >= kMaxDevices) return DSTIR_ERANGE;
-    if (!g_scratch_ptr[dev]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
-        if (e != cudaSuccess || p == nullptr) return DSTIR_ECUDA;
-        g_scratch_ptr[dev] = static_cast<unsigned char*>(p);
-    }
-    *out = g_scratch_ptr[dev];
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_static_scratch);
+    if (e != cudaSuccess || p == nullptr) return DSTIR_ECUDA;
+    *out = static_cast<unsigned char*>(p);
     return DSTIR_OK;
 }
 
@@ -123,10 +118,16 @@ extern "C" int dstir_substep_static(const DstirSceneDesc* scene, const float* pa
         d.model < 0 || d.model > 2 || d.rod_mode < 0 || d.rod_mode > 1 || d.j_mode < 0 || d.j_mode > 1 ||
         (d.rod_mode == DSTIR_ROD_CYLINDER && d.n_rod != 0))
         return DSTIR_EINVAL;
+    // per-axis bound first: n_grid^3 is only formed once it cannot overflow
+    if (d.n_grid > kMaxAxis) return DSTIR_ERANGE;
     const long long G = (long long)d.n_grid * d.n_grid * d.n_grid;
     const long long N = (long long)d.n_liquid + d.n_rod + d.n_container;
     if (G > kMaxNodes || N > kMaxParticles) return DSTIR_ERANGE;
     if (N == 0) return DSTIR_OK;
+    // an error left pending by earlier work on this thread is not ours to
+    // clear; report it before queueing anything, so that the checks after our
+    // own launches see only our own errors
+    if (cudaPeekAtLastError() != cudaSuccess) return DSTIR_ECUDA;
     unsigned char* base = nullptr;
     int rc = scratch_for_current_device(&base);
     if (rc) return rc;

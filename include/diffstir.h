@@ -86,7 +86,9 @@ typedef struct DstirHandle DstirHandle;
 /* Create a simulator for `batch` scenes able to run up to `max_steps`
  * substeps per rollout.  Replaces the field allocation of
  * src/simulator/initialization.py:123-165 (time-indexed fields become K-step
- * checkpoints owned by the handle). */
+ * checkpoints owned by the handle).  Each scene has 4 <= n_grid <= 1024, and
+ * the batch's grid nodes together (sum of n_grid^3) must not exceed INT_MAX,
+ * else DSTIR_ERANGE with *out NULL. */
 int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
                  DstirHandle** out);
 void dstir_destroy(DstirHandle* h);
@@ -205,10 +207,15 @@ int dstir_svd3_backward(const float* gU, const float* gS, const float* gV, const
  *    state_in / state_out [24][n] (component-major: x0..2 v0..2 C00..C22
  *    F00..F22, component c of particle p at c*n + p; must not overlap),
  *    force_out [3] (the substep's rod reaction force): device pointers.
- *  - Limits: n_grid <= 64 and n <= 1048576, else DSTIR_ERANGE.
- *  - Calls share the static array: calls that overlap on the GPU race; the
- *    first call on a device looks the array up and should precede any stream
- *    capture.  Device status flags are not reported. */
+ *  - Limits: n_grid <= 64 and n <= 1048576, else DSTIR_ERANGE (checked
+ *    before anything is queued).
+ *  - Calls share the static array: calls that overlap on the GPU race.  Every
+ *    call looks up the array's device address on the current device
+ *    (cudaGetSymbolAddress, which allocates nothing); the first call on a
+ *    device may load the module and should precede any stream capture.
+ *  - A CUDA error still pending on the calling thread from earlier work is
+ *    reported as DSTIR_ECUDA before anything is queued and left pending for
+ *    the caller.  Device status flags are not reported. */
 int dstir_substep_static(const DstirSceneDesc* scene, const float* params, const float* traj2,
                          const float* state_in, float* state_out, float* force_out, void* stream);
 
