@@ -96,6 +96,12 @@ def parse():
     ap.add_argument('--no-plain', action='store_true', help='skip the plain single-scene comparison')
     ap.add_argument('--no-kept', action='store_true', help='skip the kept-grids measurement')
     ap.add_argument('--fd-h', type=float, default=1e-3, help='relative step of the gradient check')
+    ap.add_argument('--no-fp64', action='store_true', help='skip the FP64 oracle gradient check')
+    ap.add_argument('--fp64-substeps', type=int, default=400, help='horizon of the FP64 oracle gradient check')
+    ap.add_argument('--no-batched', action='store_true', help='skip the batched 64-scene leg')
+    ap.add_argument('--batched-config', default='C3', help='configuration of the batched leg')
+    ap.add_argument('--batched-steps', type=int, default=2, help='timed gradient evaluations of the batched leg')
+    ap.add_argument('--plain-evals', type=int, default=3, help='timed gradient evaluations of the plain leg')
     return ap.parse_args()
 
 
@@ -247,6 +253,197 @@ def cpu_sample(sc, T_sample, threads):
     return time.perf_counter() - t0
 
 
+def oracle_segments(desc, p, traj, T, x0, K, threads, w=None):
+    """FP64 oracle rollout of T substeps chained over K-substep segments (the
+    oracle keeps every state of a call, so long rollouts of large scenes run
+    segment by segment).  Without ``w``: returns the forces [T,3].  With ``w``
+    = dL/dforce [T,3]: also runs the reverse pass segment by segment, last to
+    first, each seeded with the state adjoint the later segment produced, and
+    returns (forces, dL/dparams[4])."""
+    import oracle
+    N = x0.shape[0]
+    state = np.zeros((N, 24))
+    state[:, 0:3] = x0
+    state[:, 15:24] = np.eye(3).reshape(1, 9)
+    starts, ckpts, forces = list(range(0, T, K)), [], []
+    for s0 in starts:
+        L = min(K, T - s0)
+        ckpts.append(state)
+        f, state, rc = oracle.rollout_last(desc, p, traj[s0:s0 + L + 1], L, state[:, 0:3], state[:, 3:6],
+                                           state[:, 6:15], state[:, 15:24], threads=threads)
+        forces.append(f)
+    force = np.concatenate(forces, 0)
+    if w is None:
+        return force
+    dp = np.zeros(4)
+    seed = None
+    for s0, st in reversed(list(zip(starts, ckpts))):
+        L = min(K, T - s0)
+        _, dps, seed, _ = oracle.grad_seeded(desc, p, traj[s0:s0 + L + 1], L, st[:, 0:3], w[s0:s0 + L], seed,
+                                             st[:, 3:6], st[:, 6:15], st[:, 15:24], threads=threads)
+        dp += dps
+    return force, dp
+
+
+def fp64_grad_check(sc, p32, target32, Ts, norm, gpu_dp, free, names, h_rel, threads, K=50):
+    """The GPU adjoint of scene 0's force loss over the first Ts substeps
+    against the FP64 oracle: its adjoint (the reverse pass of the oracle's
+    FP64 rollout) and its central differences at h = h_rel x |param|.  The
+    oracle runs on the same float32 inputs the GPU got."""
+    t0 = time.perf_counter()
+    desc = sc.desc
+    x0 = np.asarray(sc.x0(), np.float32).astype(np.float64)
+    traj = np.asarray(sc.trajectory[:Ts + 1], np.float32).astype(np.float64)
+    p = np.asarray(p32, np.float32).astype(np.float64)
+    tgt = np.asarray(target32, np.float64)[:Ts]
+
+    def loss_of(force):
+        d = (force - tgt)[:, 0::2]
+        return float((d * d).sum() / norm)
+
+    f64 = oracle_segments(desc, p, traj, Ts, x0, K, threads)
+    w = np.zeros((Ts, 3))
+    w[:, 0::2] = 2.0 * (f64 - tgt)[:, 0::2] / norm
+    _, dp64 = oracle_segments(desc, p, traj, Ts, x0, K, threads, w)
+    out = {'what': 'GPU adjoint (FP32) of scene 0 against the FP64 oracle over the first %d substeps: the '
+                   'oracle\'s own reverse pass, and its central differences at h = %g x |param|' % (Ts, h_rel),
+           'substeps': Ts, 'threads': threads, 'gpu_adjoint': {}, 'fp64_adjoint': {}, 'fp64_fd': {},
+           'rel_err_gpu_vs_fp64_adjoint': {}, 'rel_err_gpu_vs_fp64_fd': {}, 'rel_err_fp64_adjoint_vs_fd': {}}
+    for i in free:
+        h = h_rel * max(abs(p[i]), 1e-3)
+        pp, pm = p.copy(), p.copy()
+        pp[i] += h
+        pm[i] -= h
+        fd = (loss_of(oracle_segments(desc, pp, traj, Ts, x0, K, threads)) -
+              loss_of(oracle_segments(desc, pm, traj, Ts, x0, K, threads))) / (2.0 * h)
+        g, a = float(gpu_dp[i]), float(dp64[i])
+        nm = names[i]
+        out['gpu_adjoint'][nm], out['fp64_adjoint'][nm], out['fp64_fd'][nm] = g, a, fd
+        out['rel_err_gpu_vs_fp64_adjoint'][nm] = abs(g - a) / max(abs(a), 1e-30)
+        out['rel_err_gpu_vs_fp64_fd'][nm] = abs(g - fd) / max(abs(fd), 1e-30)
+        out['rel_err_fp64_adjoint_vs_fd'][nm] = abs(a - fd) / max(abs(fd), 1e-30)
+    out['rel_err_max'] = max(max(out['rel_err_gpu_vs_fp64_adjoint'].values()),
+                             max(out['rel_err_gpu_vs_fp64_fd'].values()))
+    out['seconds'] = time.perf_counter() - t0
+    return out
+
+
+def plain_leg(scenes, targets, params, T, ckpt, n_evals, stream):
+    """The reference's algorithm on the GPU, one scene at a time: per-particle
+    scalar float atomics, particles in generation order, no graph.  Times one
+    gradient evaluation of each of ``n_evals`` scenes (cycling through
+    ``scenes``) after an untimed one."""
+    import torch
+    from diffstir_gb300.simulator import Simulator
+    sims = {}
+    evals = [(i % len(scenes)) for i in range(n_evals)]
+
+    def one(i):
+        if i not in sims:
+            sims[i] = Simulator([scenes[i]], max_steps=T, options={'p2g': 0, 'graph': 0, 'fuse': 0, 'fuse_adj': 0},
+                                reorder=False)
+        ps = sims[i]
+        ps.set_params(params[i:i + 1].contiguous())
+        ps.reset()
+        f = ps.forward(T, ckpt_every=ckpt, record=True)
+        diff = (f - targets[i:i + 1])[..., 0::2]
+        dF = torch.zeros_like(f)
+        dF[..., 0::2] = 2.0 * diff / diff.numel()
+        return ps.backward(dF)
+
+    one(evals[0])
+    for i in set(evals):
+        if i not in sims:
+            one(i)
+    torch.cuda.synchronize()
+    q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    q0.record(stream)
+    for i in evals:
+        one(i)
+    q1.record(stream)
+    torch.cuda.synchronize()
+    ms = q0.elapsed_time(q1)
+    for ps in sims.values():
+        ps.close()
+    n_ps = sum(scenes[i].n_particles for i in evals) * T
+    return {'grad_evals_per_s': n_evals * 1e3 / ms, 'value': n_ps / (ms / 1e3), 'unit': UNIT,
+            'ms_per_grad_eval': ms / n_evals, 'timed_grad_evals': n_evals,
+            'scenes': sorted(set(evals)), 'particles': [scenes[i].n_particles for i in sorted(set(evals))],
+            'what': 'one scene at a time, scalar atomics, generation order, no graph; %d timed gradient '
+                    'evaluations' % n_evals}
+
+
+def batched_leg(args, rank, world, dev, stream):
+    """The batched workload (64 scenes of 64^3 with uneven fill heights and
+    Herschel-Bulkley parameters, 1000 substeps): gradient evaluations of all
+    scenes in one handle, against the plain single-scene GPU rollout of the
+    same scenes."""
+    import torch
+    from diffstir_gb300 import scene as S
+    from diffstir_gb300 import autotune
+    from diffstir_gb300.simulator import Simulator
+    cfg = S.CONFIGS[args.batched_config]
+    T, ckpt, B = cfg['n_steps'], cfg['ckpt'], cfg.get('batch', 1)
+    t_build = time.perf_counter()
+    scenes = [S.synthetic_scene(args.batched_config, seed=rank * B + b, n_steps=T) for b in range(B)]
+    # the tuner's candidates that win for batches of 64^3 scenes
+    opts = autotune.autotune(scenes, candidates=[c for c in autotune.CANDIDATES
+                                                 if c.get('p2g') == 4 and c.get('tight') == 2])
+    sim = Simulator(scenes, max_steps=T, options=opts)
+    rng = np.random.default_rng(2000 + rank)
+    true_p = torch.tensor(np.stack([S.draw_config_params(args.batched_config, rng) for _ in range(B)]),
+                          dtype=torch.float32, device=dev)
+    sim.set_params(true_p)
+    sim.reset()
+    target = sim.forward(T).clone()
+    params = torch.tensor(np.stack([s.params for s in scenes]), dtype=torch.float32, device=dev)
+    build_s = time.perf_counter() - t_build
+
+    def grad_eval():
+        sim.set_params(params)
+        sim.reset()
+        f = sim.forward(T, ckpt_every=ckpt, record=True)
+        diff = (f - target)[..., 0::2]
+        dF = torch.zeros_like(f)
+        dF[..., 0::2] = 2.0 * diff / diff.numel()
+        return sim.backward(dF)
+
+    grad_eval()
+    torch.cuda.synchronize()
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.batched_steps):
+        grad_eval()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.batched_steps
+    if world > 1:
+        import torch.distributed as dist
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    st = sim.status()
+    N = sum(s.n_particles for s in scenes)
+    opt_used = {k: sim.get_option(k) for k in ('p2g', 'gblock', 'tight', 'lsort', 'lstage', 'pdl', 'overlap')}
+    sim.close()
+    del sim
+    torch.cuda.empty_cache()
+    plain = plain_leg(scenes, target, params, T, ckpt, max(args.plain_evals, 3), stream)
+    ge = world * B * 1e3 / ms
+    return {'workload': '%s: %d scenes of %d^3 grid, %d particles in all (%d..%d per scene), %d substeps, '
+                        'checkpoint every %d, Herschel-Bulkley fluid; forward + checkpointed adjoint of all scenes '
+                        'per step' % (args.batched_config, B, cfg['n_grid'], N, min(s.n_particles for s in scenes),
+                                      max(s.n_particles for s in scenes), T, ckpt),
+            'grad_evals_per_s': ge, 'value': world * N * T / (ms / 1e3), 'unit': UNIT, 'ms_per_step': ms,
+            'timed_steps': args.batched_steps, 'options': opt_used, 'status_flags': int(st),
+            'setup_s': build_s, 'plain': plain,
+            'batched_over_plain': {'grad_evals_per_s': ge / plain['grad_evals_per_s'],
+                                   'particle_substeps_per_s': world * N * T / (ms / 1e3) / plain['value']}}
+
+
 def run_reference(args):
     world, rank, local = dist_setup(args)
     if rank != 0:
@@ -358,13 +555,25 @@ def run_ours(args):
     # bracketed by events on the launching stream (kept out of the timed steps,
     # whose value the event records would perturb for small scenes; graph
     # replay is switched off for this pass so that each launch is visible)
+    # A second pass runs with the overlap of the reverse pass off, so that
+    # each kernel's mean launch time is not inflated by kernels of the other
+    # stream queued beside it; the roofline uses that pass.
     graph_was = sim.get_option('graph')
+    overlap_was = sim.get_option('overlap')
     sim.set_option('graph', 0)
-    sim.set_option('profile', 1)
-    grad_eval(params)
-    torch.cuda.synchronize()
-    prof = {k: (sim.get_option('prof_ns:' + k) / 1e6, sim.get_option('prof_count:' + k)) for k in KERNELS}
-    sim.set_option('profile', 0)
+
+    def profiled_pass():
+        sim.set_option('profile', 1)
+        grad_eval(params)
+        torch.cuda.synchronize()
+        pr = {k: (sim.get_option('prof_ns:' + k) / 1e6, sim.get_option('prof_count:' + k)) for k in KERNELS}
+        sim.set_option('profile', 0)
+        return pr
+
+    prof_ovl = profiled_pass()
+    sim.set_option('overlap', 0)
+    prof = profiled_pass()
+    sim.set_option('overlap', overlap_was)
     sim.set_option('graph', graph_was)
     if world > 1:
         import torch.distributed as dist
@@ -431,6 +640,7 @@ def run_ours(args):
     # `loss_noise_rel` is that variation between two identical rollouts, and
     # `fd_noise_rel` what it contributes to a difference quotient at each step.
     grad_check = None
+    fp64_in = None
     if not args.no_fd:
         _, dp_adj = grad_eval(params)
         free = [0, 1, 2] if ys else [0, 2]
@@ -471,6 +681,8 @@ def run_ours(args):
             dF = torch.zeros_like(f)
             dF[..., 0::2] = 2.0 * diff / float(B * Ts * 2)
             dp_s = sim.backward(dF)
+            fp64_in = (Ts, dp_s[0].double().cpu().numpy(), fs_t[0].double().cpu().numpy(), float(B * Ts * 2), free,
+                       names)
             short = {}
             for hr in sorted({args.fd_h, 1e-2}):
                 errs = {}
@@ -503,31 +715,7 @@ def run_ours(args):
     # atomics, particles in generation order, no graph
     plain = None
     if not args.no_plain:
-        ps = Simulator([sc], max_steps=T, options={'p2g': 0, 'graph': 0, 'fuse': 0, 'fuse_adj': 0}, reorder=False)
-        tgt1 = target[:1].contiguous()
-        p1 = params[:1].contiguous()
-
-        def plain_eval():
-            ps.set_params(p1)
-            ps.reset()
-            f = ps.forward(T, ckpt_every=ckpt, record=True)
-            diff = (f - tgt1)[..., 0::2]
-            dF = torch.zeros_like(f)
-            dF[..., 0::2] = 2.0 * diff / diff.numel()
-            return ps.backward(dF)
-
-        plain_eval()
-        torch.cuda.synchronize()
-        q0, q1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        q0.record(stream)
-        plain_eval()
-        q1.record(stream)
-        torch.cuda.synchronize()
-        pms = q0.elapsed_time(q1)
-        ps.close()
-        plain = {'grad_evals_per_s': 1e3 / pms, 'value': sc.n_particles * T / (pms / 1e3), 'unit': UNIT,
-                 'ms_per_grad_eval': pms,
-                 'what': 'scene 0 alone, scalar atomics, generation order, no graph, 1 timed gradient evaluation'}
+        plain = plain_leg([sc], target[:1].contiguous(), params[:1].contiguous(), T, ckpt, args.plain_evals, stream)
 
     # e2e through the public API with pinned host inputs / host results
     e2e = None
@@ -568,6 +756,24 @@ def run_ours(args):
         e2e = {'value': n_total * T / (e2e_ms / 1e3), 'unit': UNIT, 'h2d_bytes_per_step': int(h2d),
                'd2h_bytes_per_step': int(d2h), 'ms_per_step': e2e_ms}
 
+    status_all = int(st) | int(sim.status())
+    opts_used = {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather',
+                                                'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder',
+                                                'store_grids', 'overlap', 'lsort', 'pdl', 'lstage')}
+    scatter_variant, scatter_fused = sim.get_option('p2g'), sim.get_option('fuse')
+    sim.close()
+    del sim
+    torch.cuda.empty_cache()
+
+    # the batched workload: many scenes per handle against the plain rollout
+    batched = None
+    if not args.no_batched and args.config != args.batched_config:
+        try:
+            batched = batched_leg(args, rank, world, dev, stream)
+        except Exception as exc:  # reported in the line; the headline stands
+            batched = {'error': '%s: %s' % (type(exc).__name__, exc)}
+            torch.cuda.empty_cache()
+
     if rank != 0:
         return 0
 
@@ -592,7 +798,7 @@ def run_ours(args):
     # (committed ncu summary) over the live mean launch time, against the RED
     # sector rate measured on this GPU
     red_roof = None
-    if sim.get_option('p2g') in (1, 4) and not sim.get_option('fuse'):
+    if scatter_variant in (1, 4) and not scatter_fused:
         peak_red = red_peak(max(s.desc.n_grid ** 3 for s in scenes))  # one scene's grid: L2-resident
         red_roof = {'unit': 'RED sectors/s', 'peak': peak_red,
                     'peak_kind': 'measured: 32 consecutive float4 nodes per warp RED, L2-resident grid'}
@@ -614,7 +820,24 @@ def run_ours(args):
                          '(ncu sm__inst_executed_pipe_fma, of peak sustained active)'}
     # whole-step algorithmic bytes: forward 192 N + 56 G, adjoint 480 N + 112 G per substep
     step_bytes = T * ((192 + 480) * N + (56 + 112) * G)
-    kernel_share = {k: round(prof[k][0] / max(sum(v[0] for v in prof.values()), 1e-9), 4) for k in KERNELS}
+    kernel_share = {k: round(prof_ovl[k][0] / max(sum(v[0] for v in prof_ovl.values()), 1e-9), 4) for k in KERNELS}
+    kernel_us = {'serial': {k: round(prof[k][0] * 1e3 / prof[k][1], 2) for k in KERNELS if prof[k][1]},
+                 'overlapped': {k: round(prof_ovl[k][0] * 1e3 / prof_ovl[k][1], 2) for k in KERNELS if prof_ovl[k][1]},
+                 'what': 'mean CUDA-event time per launch (us) in one profiled gradient evaluation without graphs: '
+                         '"serial" with the reverse pass on one stream (the roofline uses it), "overlapped" with '
+                         'the recompute of the next segment on a second stream, as in the timed steps; *_rc = the '
+                         'segment recompute'}
+
+    # FP64 oracle check of the gradient (host cores, after all GPU timing)
+    if fp64_in is not None and not args.no_fp64:
+        Ts, dp0, tgt0, norm, free, names = fp64_in
+        Ts_fp = min(args.fp64_substeps, Ts)
+        if Ts_fp == Ts:
+            try:
+                grad_check['fp64'] = fp64_grad_check(sc, params[0].cpu().numpy(), tgt0, Ts, norm, dp0, free, names,
+                                                     args.fd_h, os.cpu_count() or 1, K=ckpt)
+            except Exception as exc:
+                grad_check['fp64'] = {'error': '%s: %s' % (type(exc).__name__, exc)}
 
     cpu = None
     if not args.no_cpu:
@@ -632,7 +855,11 @@ def run_ours(args):
         'config': {'workload': wl, 'grid': G, 'particles': N, 'substeps': T, 'ckpt_every': ckpt,
                    'scenes_per_gpu': B, 'parallelism': 'scene-sharded (%d scene(s) per GPU)' % B,
                    'l2': 'inputs larger than L2 (checkpoints + segment states ~%.1f GB per step)' %
-                         ((T // ckpt + ckpt) * N * 96 / 1e9)},
+                         ((T // ckpt + ckpt) * N * 96 / 1e9),
+                   'cpu_timings': 'cpu_baseline and the reference arm time the first %d / %d substeps of the %d '
+                                  '(forward + adjoint) and report them per particle-substep: a per-substep '
+                                  'extrapolation of a prefix, taken before the fluid reaches the walls'
+                                  % (min(args.cpu_sample, T), min(args.ref_sample, T), T)},
         'grad_evals_per_s': world * B * 1e3 / ms,
         'forward_value': n_total * T / (fwd_ms / 1e3),
         'kept_grids': kept,
@@ -641,16 +868,16 @@ def run_ours(args):
         'forward_adjoint_roofline_frac': step_bytes / (ms / 1e3) / 1e9 / hbm,
         'roofline': roof,
         'kernel_time_share': kernel_share,
+        'kernel_us_per_launch': kernel_us,
+        'batched': batched,
         'roofline_l2_red': red_roof,
         'roofline_fp32': fp32_roof,
         'cpu_baseline': cpu,
         'e2e': e2e,
         'gpu_launches': int(launches),
-        'options': {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather',
-                                                   'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder', 'store_grids', 'overlap',
-                                                   'lsort', 'pdl', 'lstage')},
+        'options': opts_used,
         'clocks': clk,
-        'status_flags': int(st),
+        'status_flags': status_all,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

@@ -11,7 +11,10 @@ src/simulator/simulation_functions.py with a hand-derived adjoint) into
 sticky top (a node of the top band loses its whole velocity when v_y > 0,
 simulation_functions.py:221-224) by a clamp of v_y alone; it exists only to
 show that this discontinuous rule is what separates adjoint and difference
-quotients once the fluid reaches the top band.
+quotients once the fluid reaches the top band.  The diagnostic variant
+``branch_counts`` counts how often each boundary rule of grid_op
+(simulation_functions.py:204-224) changed the velocity of a node with mass
+(:func:`branch_counts`), to show which rules a fixture's rollout exercises.
 """
 
 import ctypes as C
@@ -25,7 +28,10 @@ SRC = os.path.join(HERE, 'oracle.cpp')
 OUT_DIR = os.path.join(HERE, '_build')
 LIB = os.path.join(OUT_DIR, 'liboracle.so')
 VARIANTS = {None: ([], 'liboracle.so'),
-            'continuous_top': (['-DORACLE_CONTINUOUS_TOP'], 'liboracle_continuous_top.so')}
+            'continuous_top': (['-DORACLE_CONTINUOUS_TOP'], 'liboracle_continuous_top.so'),
+            'branch_counts': (['-DORACLE_BRANCH_COUNTS'], 'liboracle_branch_counts.so')}
+BRANCHES = ('container_projection', 'wall_i_low', 'wall_i_high', 'wall_k_low', 'wall_k_high', 'wall_j_low',
+            'sticky_top', 'nodes_with_mass')
 
 _libs = {}
 
@@ -175,6 +181,18 @@ def svd3_backward(gU, gS, gV, U, S, V):
     gA = np.zeros((n, 9))
     lib.oracle_svd3_backward_f64(_p(gU), _p(gS), _p(gV), _p(U), _p(S), _p(V), _p(gA), n)
     return gA.reshape(n, 3, 3)
+
+
+def branch_counts():
+    """Counts of the boundary rules taken since the last call (``branch_counts``
+    variant, forward substeps of every rollout), as a dict keyed by
+    :data:`BRANCHES`; clears them."""
+    lib = load('branch_counts')
+    lib.oracle_branch_counts.argtypes = [C.POINTER(C.c_longlong), C.c_int]
+    lib.oracle_branch_counts.restype = C.c_int
+    out = (C.c_longlong * len(BRANCHES))()
+    lib.oracle_branch_counts(out, len(BRANCHES))
+    return dict(zip(BRANCHES, [int(v) for v in out]))
 
 
 def max_threads():

@@ -37,6 +37,23 @@
 
 namespace {
 
+#ifdef ORACLE_BRANCH_COUNTS
+// Diagnostic build: how often each boundary rule of grid_op (:204-224)
+// changed the velocity of a node with mass, summed over the forward substeps
+// of every rollout since the last oracle_branch_counts call.  Index:
+// 0 container projection, 1 wall i<b, 2 wall i>n-b, 3 wall k<b, 4 wall k>n-b,
+// 5 wall j<b, 6 sticky top, 7 nodes with mass visited.
+constexpr int NBRANCH = 8;
+long long g_branch[NBRANCH];
+inline void count_branch(int b) {
+#pragma omp atomic
+    g_branch[b]++;
+}
+#define BRANCH(b) count_branch(b)
+#else
+#define BRANCH(b) ((void)0)
+#endif
+
 constexpr int NS = 24;  // per-particle state: x3 v3 C9 F9
 constexpr int OX = 0, OV = 3, OC = 6, OF = 15;
 
@@ -441,6 +458,8 @@ struct Sim {
             const R* gn = g + idx * 4;
             R inv_m = R(1) / (gn[3] + R(1e-10));
             R v[3] = {inv_m * gn[0], inv_m * gn[1], inv_m * gn[2]};
+            const bool massive = gn[3] > R(0);
+            if (massive) BRANCH(7);
             if (d.container_wall) {
                 R r = R(d.container_r);
                 R dist[3] = {R(i) * dx - R(d.container_cx), R(0), R(k) * dx - R(d.container_cz)};
@@ -451,19 +470,23 @@ struct Sim {
                     R dot = v[0] * u0 + v[2] * u2;
                     v[0] -= u0 * dot;
                     v[2] -= u2 * dot;
+                    if (massive && dot != R(0)) BRANCH(0);
                 }
             }
             int b = d.bound;
-            if (i < b && v[0] < 0) v[0] = 0;
-            if (i > n - b && v[0] > 0) v[0] = 0;
-            if (k < b && v[2] < 0) v[2] = 0;
-            if (k > n - b && v[2] > 0) v[2] = 0;
-            if (j < b && v[1] < 0) v[1] = 0;
+            if (i < b && v[0] < 0) { v[0] = 0; if (massive) BRANCH(1); }
+            if (i > n - b && v[0] > 0) { v[0] = 0; if (massive) BRANCH(2); }
+            if (k < b && v[2] < 0) { v[2] = 0; if (massive) BRANCH(3); }
+            if (k > n - b && v[2] > 0) { v[2] = 0; if (massive) BRANCH(4); }
+            if (j < b && v[1] < 0) { v[1] = 0; if (massive) BRANCH(5); }
 #ifdef ORACLE_CONTINUOUS_TOP
             // diagnostic build: a plain clamp instead of the sticky top
             if (j > n - b && v[1] > 0) v[1] = 0;
 #else
-            if (j > n - b && v[1] > 0) { v[0] = 0; v[1] = 0; v[2] = 0; }  // sticky top, :221-224
+            if (j > n - b && v[1] > 0) {  // sticky top, :221-224
+                v[0] = 0; v[1] = 0; v[2] = 0;
+                if (massive) BRANCH(6);
+            }
 #endif
             if (cyl) {
                 R ddx = R(i) * dx - rc[0], ddz = R(k) * dx - rc[2];
@@ -1011,6 +1034,18 @@ void oracle_svd3_backward_f64(const double* gU, const double* gS, const double* 
     for (int64_t i = 0; i < n; ++i)
         svd3_backward_d(gU + i * 9, gS + i * 3, gV + i * 9, U + i * 9, S + i * 3, V + i * 9, gA + i * 9);
 }
+
+#ifdef ORACLE_BRANCH_COUNTS
+// Copies the branch counters (NBRANCH entries, see g_branch) to out, up to n
+// of them, and clears them; returns NBRANCH.
+int oracle_branch_counts(long long* out, int n) {
+    for (int i = 0; i < NBRANCH; ++i) {
+        if (out && i < n) out[i] = g_branch[i];
+        g_branch[i] = 0;
+    }
+    return NBRANCH;
+}
+#endif
 
 int oracle_max_threads(void) {
 #ifdef _OPENMP

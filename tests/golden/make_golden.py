@@ -97,16 +97,30 @@ def scene_record(sf):
 
 
 def run_fixture(ref_root, name, n_grid, n_liq, n_op, n_cont, T, seed, prec, models,
-                with_grad, out_dir):
+                with_grad, out_dir, extra=None):
+    """``extra`` (optional): 'dt' replaces simulation_setting.dt, 'scene'
+    updates scene_information, 'traj_quantum' rounds the trajectory to
+    multiples of that power of two, so that the reference's centring
+    (initialization.py:74-77) stays exact and the processed trajectory is
+    exactly representable in float32: the rod velocity (q[f+1]-q[f])/dt
+    (simulation_functions.py:266) then needs no float32 rounding of q, and a
+    float32 simulator can be compared with this fixture directly."""
+    extra = extra or {}
     cfg = json.load(open(os.path.join(ref_root, 'config', 'arguments.json')))
     ss = cfg['simulation_setting']
     ss['n_grid'] = n_grid
     ss['n_model_particles_generated'] = n_liq
     ss['n_operator_model_particles_generated'] = n_op
     ss['n_container_model_particles_generated'] = n_cont
+    if 'dt' in extra:
+        ss['dt'] = extra['dt']
+    cfg['scene_information'].update(extra.get('scene', {}))
     traj_full = np.load(os.path.join(ref_root, 'data', 'traj.npy'))
     force_full = np.load(os.path.join(ref_root, 'data', 'force.npy'))
     traj = traj_full[:T + 1].copy()
+    if 'traj_quantum' in extra:
+        q = extra['traj_quantum']
+        traj = np.round(traj / q) * q
     force = force_full[:T + 1].copy()
     rng = np.random.default_rng(1000 + seed)
     out = {}
@@ -157,6 +171,7 @@ def run_fixture(ref_root, name, n_grid, n_liq, n_op, n_cont, T, seed, prec, mode
             out[p + 'grad_C1'] = sf.C.grad.to_numpy()[1] if sf.max_steps > 1 else np.zeros(0)
         print('%s model %d: %.1fs loss=%r' % (name, model, time.time() - t0,
                                                float(out[p + 'loss'])), flush=True)
+    out['meta_config'] = np.array(json.dumps(cfg))
     out['meta_prec'] = np.array(prec)
     out['meta_seed'] = np.int64(seed)
     out['meta_T'] = np.int64(T)
@@ -165,11 +180,21 @@ def run_fixture(ref_root, name, n_grid, n_liq, n_op, n_cont, T, seed, prec, mode
     print('wrote', path, os.path.getsize(path), 'bytes')
 
 
+# Long fixtures: a wide, tall container on a 16^3 grid, so that within 60
+# substeps at the reference's dt the fluid's nodes meet every boundary rule
+# of grid_op (the container projection with mass :205-210, the six wall
+# clamps :211-220 and the sticky top :221-224) and the rod dv (:266-270)
+# accumulates over many frames.  Trajectory rounded to multiples of 2^-24.
+LONG = {'scene': {'container_diameter': 0.74, 'liquid_height': 0.58, 'container_height': 0.6},
+        'traj_quantum': 2.0 ** -24}
+
 FIXTURES = {
-    # name: (n_grid, n_liquid, n_rod, n_container, substeps T, seed, precision, models, grad)
+    # name: (n_grid, n_liquid, n_rod, n_container, substeps T, seed, precision, models, grad[, extra])
     'ref_f64_g32': (32, 300, 40, 60, 6, 0, 'f64', (0, 1, 2), True),
     'ref_f32_g32': (32, 300, 40, 60, 6, 0, 'f32', (0, 1, 2), True),
     'ref_f64_g71': (71, 400, 50, 60, 3, 1, 'f64', (2,), True),
+    'ref_f64_g16_long': (16, 160, 16, 40, 60, 0, 'f64', (0, 1, 2), True, LONG),
+    'ref_f32_g16_long': (16, 160, 16, 40, 60, 0, 'f32', (0, 1, 2), True, LONG),
 }
 
 
@@ -178,7 +203,8 @@ def main():
     assert ref_root and os.path.isdir(ref_root), 'pass the reference checkout path'
     names = sys.argv[2:] or list(FIXTURES)
     for name in names:
-        run_fixture(ref_root, name, *FIXTURES[name], out_dir=HERE)
+        args = FIXTURES[name]
+        run_fixture(ref_root, name, *args[:9], out_dir=HERE, extra=args[9] if len(args) > 9 else None)
 
 
 if __name__ == '__main__':
