@@ -54,7 +54,7 @@ KERNEL_BYTES = {
     'p2g_adj_g2p_adj': (204, 40),
 }
 KERNELS = ['p2g', 'grid', 'g2p', 'g2p_adj', 'grid_adj', 'p2g_adj', 'bin', 'g2p_p2g', 'p2g_adj_g2p_adj', 'other',
-           'p2g_rc', 'grid_rc', 'g2p_rc', 'bin_rc', 'g2p_p2g_rc']
+           'p2g_rc', 'grid_rc', 'g2p_rc', 'bin_rc', 'g2p_p2g_rc', 'seg_fwd', 'seg_adj', 'seg_fwd_rc']
 # the in-library profiler reports the reverse pass's segment recompute under
 # <kernel>_rc; the roofline counts both launches of the same kernel together
 RC = {'p2g': 'p2g_rc', 'grid': 'grid_rc', 'g2p': 'g2p_rc', 'g2p_p2g': 'g2p_p2g_rc'}
@@ -88,6 +88,7 @@ def parse():
     ap.add_argument('--lsort', type=int, default=None, help='1: re-interleave each block before the warp scatters')
     ap.add_argument('--pdl', type=int, default=None, help='1: programmatic dependent launch of the substep kernels')
     ap.add_argument('--lstage', type=int, default=None, help='re-interleaved blocks stage their state in shared memory (bits: P2G, G2P adjoint)')
+    ap.add_argument('--persist', type=int, default=None, help='1: persistent cooperative launches per chunk / segment')
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
     ap.add_argument('--no-e2e', action='store_true')
@@ -490,7 +491,7 @@ def run_ours(args):
     sc = scenes[0]
     opts = {}
     keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather', 'fuse', 'fuse_adj', 'resort', 'tight',
-            'box', 'reorder', 'store_grids', 'overlap', 'lsort', 'pdl', 'lstage')
+            'box', 'reorder', 'store_grids', 'overlap', 'lsort', 'pdl', 'lstage', 'persist')
     explicit = any(getattr(args, k) is not None for k in keys)
     if args.autotune and not explicit:
         from diffstir_gb300 import autotune
@@ -759,7 +760,7 @@ def run_ours(args):
     status_all = int(st) | int(sim.status())
     opts_used = {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather',
                                                 'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder',
-                                                'store_grids', 'overlap', 'lsort', 'pdl', 'lstage')}
+                                                'store_grids', 'overlap', 'lsort', 'pdl', 'lstage', 'persist')}
     scatter_variant, scatter_fused = sim.get_option('p2g'), sim.get_option('fuse')
     sim.close()
     del sim
@@ -784,16 +785,18 @@ def run_ours(args):
             for k in KERNEL_BYTES}
     dom = max(KERNEL_BYTES, key=lambda k: both[k][0])
     tot_ms, cnt = both[dom]
-    avg_s = tot_ms / 1e3 / max(cnt, 1)
-    bp, bn = KERNEL_BYTES[dom]
-    alg = bp * NL + bn * G
     hbm, peak_kind = peaks()
-    achieved = alg / avg_s / 1e9
     wl = workload_name(args, scenes, T, ckpt)
-    roof = {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
-            'frac': achieved / hbm, 'peak_kind': peak_kind, 'alg_bytes_per_launch': alg,
-            'avg_launch_us': avg_s * 1e6, 'traffic': ncu_traffic(dom, args.config),
-            'launches_per_step': cnt}
+    roof = None
+    if cnt:  # (the persistent launches of option persist carry no per-kernel split)
+        avg_s = tot_ms / 1e3 / cnt
+        bp, bn = KERNEL_BYTES[dom]
+        alg = bp * NL + bn * G
+        achieved = alg / avg_s / 1e9
+        roof = {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': hbm, 'unit': 'GB/s',
+                'frac': achieved / hbm, 'peak_kind': peak_kind, 'alg_bytes_per_launch': alg,
+                'avg_launch_us': avg_s * 1e6, 'traffic': ncu_traffic(dom, args.config),
+                'launches_per_step': cnt}
     # atomic roofline of the two scatter kernels: vector-RED sectors per launch
     # (committed ncu summary) over the live mean launch time, against the RED
     # sector rate measured on this GPU

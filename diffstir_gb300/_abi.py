@@ -10,6 +10,7 @@ DSTIR_ESTATE = -4
 DSTIR_ERANGE = -5
 
 DSTIR_STATUS_NAN = 1
+DSTIR_STATUS_TIMEOUT = 4
 DSTIR_STATUS_OUT_OF_GRID = 2
 
 MODEL_CARREAU, MODEL_CROSS, MODEL_HB = 0, 1, 2

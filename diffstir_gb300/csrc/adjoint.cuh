@@ -15,16 +15,17 @@
 
 namespace dstir {
 
-template <bool SVDJ>
+// NC: load policy of the state reads (see ldp in device_util.cuh).
+template <bool SVDJ, bool NC = true>
 __device__ __forceinline__ void p2g_adj_affine(const float* cur, long long stride, const SceneDev& s,
                                                const float* prm, int model, long long p, int kind, float& m,
                                                float mv[3], float A[9]) {
     float v[3], C[9];
-    load3(cur, stride, OV, p, v);
-    load9(cur, stride, OC, p, C);
+    load3<NC>(cur, stride, OV, p, v);
+    load9<NC>(cur, stride, OC, p, C);
     if (kind == KIND_LIQUID) {
         float F[9];
-        load9(cur, stride, OF, p, F);
+        load9<NC>(cur, stride, OF, p, F);
         LiquidP2G q;
         liquid_p2g<SVDJ>(s, model, prm, v, C, F, q);
         m = s.m_liq;
@@ -75,8 +76,9 @@ __device__ __forceinline__ void p2g_adj_node(float W, float dWx, float dWy, floa
 // so a node costs its weight products, one float4 load, a 4-term dot product
 // for Wb and a handful of adds, instead of the three 3x3 products of
 // p2g_adj_node.  `pmb` is the P/M-adjoint grid, `row0` the node index of the
-// stencil base (k innermost).
-__device__ __forceinline__ void p2g_adj_gather(const float4* __restrict__ pmb, const SceneDev& s,
+// stencil base (k innermost).  NC: load policy of the pmb reads.
+template <bool NC = true>
+__device__ __forceinline__ void p2g_adj_gather(const float4* pmb, const SceneDev& s,
                                                const int base[3], const float fx[3], const float w[3][3],
                                                const float dw[3][3], float m, const float mv[3],
                                                const float A[9], bool liquid, float Ab[9], float vvb[3],
@@ -104,7 +106,7 @@ __device__ __forceinline__ void p2g_adj_gather(const float4* __restrict__ pmb, c
             for (int a = 0; a < 3; ++a) r[a] = c[a] + (float)i * Ad[a * 3 + 0] + (float)j * Ad[a * 3 + 1];
 #pragma unroll
             for (int k = 0; k < 3; ++k) {
-                const float4 g = __ldg(rowp + k);
+                const float4 g = ldp<NC>(rowp + k);
                 const float W = wij * w[k][2];
                 const float rk0 = r[0] + (float)k * Ad[2], rk1 = r[1] + (float)k * Ad[5], rk2 = r[2] + (float)k * Ad[8];
                 const float Wb = g.w * m + g.x * rk0 + g.y * rk1 + g.z * rk2;
@@ -140,7 +142,7 @@ __device__ __forceinline__ void p2g_adj_gather(const float4* __restrict__ pmb, c
 
 // The adjoint of the state at substep f (xb, vb, Cb, Fb) from the stencil
 // gather results; parameter partials are added to pg.
-template <bool SVDJ>
+template <bool SVDJ, bool NC = true>
 __device__ __forceinline__ void p2g_adj_core(const AdjArgs& a, const SceneDev& s, const float* prm, int model,
                                              long long p, int kind, float m, const float Ab[9], const float vvb[3],
                                              const float fxb[3], float pg[4], float xb[3], float vb[3], float Cb[9],
@@ -157,12 +159,12 @@ __device__ __forceinline__ void p2g_adj_core(const AdjArgs& a, const SceneDev& s
         for (int c = 0; c < 3; ++c) xb[c] = vb[c] = 0.f;
         return;
     }
-    load3(a.adj_cur, a.stride, OX, p, xb);  // G2P part, written by the G2P adjoint
+    load3<NC>(a.adj_cur, a.stride, OX, p, xb);  // G2P part, written by the G2P adjoint
 #pragma unroll
     for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
     float C[9], F[9], IC[9], Ft[9];
-    load9(a.cur, a.stride, OC, p, C);
-    load9(a.cur, a.stride, OF, p, F);
+    load9<NC>(a.cur, a.stride, OC, p, C);
+    load9<NC>(a.cur, a.stride, OF, p, F);
 #pragma unroll
     for (int i = 0; i < 9; ++i) IC[i] = s.dt * C[i] + ((i % 4 == 0) ? 1.f : 0.f);
     matmul3(IC, F, Ft);
@@ -196,7 +198,7 @@ __device__ __forceinline__ void p2g_adj_core(const AdjArgs& a, const SceneDev& s
     float trb = sigb[0] + sigb[4] + sigb[8];
     float Jb = trb * (s.bulk / 2.f) * (2.f * J - 1.f);
     float Ftb[9];
-    load9(a.adj_next, a.stride, OF, p, Ftb);  // F[f+1] = F_tmp
+    load9<NC>(a.adj_next, a.stride, OF, p, Ftb);  // F[f+1] = F_tmp
     if (SVDJ && s.j_mode == DSTIR_J_SVD) {
         float gS[3] = {Jb * sg[1] * sg[2], Jb * sg[0] * sg[2], Jb * sg[0] * sg[1]};
         float z[9], gA[9];
@@ -235,12 +237,12 @@ __device__ __forceinline__ void p2g_adj_core(const AdjArgs& a, const SceneDev& s
 }
 
 // p2g_adj_core followed by storing the whole state adjoint into a.adj_cur.
-template <bool SVDJ>
+template <bool SVDJ, bool NC = true>
 __device__ __forceinline__ void p2g_adj_finish(const AdjArgs& a, const SceneDev& s, const float* prm, int model,
                                                long long p, int kind, float m, const float Ab[9], float vvb[3],
                                                const float fxb[3], float pg[4]) {
     float xb[3], vb[3], Cb[9], Fb[9];
-    p2g_adj_core<SVDJ>(a, s, prm, model, p, kind, m, Ab, vvb, fxb, pg, xb, vb, Cb, Fb);
+    p2g_adj_core<SVDJ, NC>(a, s, prm, model, p, kind, m, Ab, vvb, fxb, pg, xb, vb, Cb, Fb);
     store3(a.adj_cur, a.stride, OX, p, xb);
     store3(a.adj_cur, a.stride, OV, p, vb);
     store9(a.adj_cur, a.stride, OC, p, Cb);

@@ -28,10 +28,11 @@ namespace {
 // (the *_rc kinds are the same kernels inside the reverse pass's segment
 // recompute; "p2g" etc. count the forward rollouts only)
 enum { K_P2G = 0, K_GRID, K_G2P, K_G2P_ADJ, K_GRID_ADJ, K_P2G_ADJ, K_BIN, K_G2P_P2G, K_P2G_ADJ_G2P_ADJ, K_OTHER,
-       K_P2G_RC, K_GRID_RC, K_G2P_RC, K_BIN_RC, K_G2P_P2G_RC, K_NUM };
-const char* const kKernelNames[K_NUM] = {"p2g",     "grid",     "g2p",    "g2p_adj", "grid_adj",
+       K_P2G_RC, K_GRID_RC, K_G2P_RC, K_BIN_RC, K_G2P_P2G_RC, K_SEG_FWD, K_SEG_ADJ, K_SEG_FWD_RC, K_NUM };
+const char* const kKernelNames[K_NUM] = {"p2g",     "grid",     "g2p",     "g2p_adj", "grid_adj",
                                          "p2g_adj", "bin",      "g2p_p2g", "p2g_adj_g2p_adj",
-                                         "other",   "p2g_rc",   "grid_rc", "g2p_rc", "bin_rc", "g2p_p2g_rc"};
+                                         "other",   "p2g_rc",   "grid_rc", "g2p_rc",  "bin_rc", "g2p_p2g_rc",
+                                         "seg_fwd", "seg_adj",  "seg_fwd_rc"};
 
 // CUDA-event timing of every launch on the launching stream.  Event pairs live
 // in a ring; a pair is read back (synchronising on its stop event) when the
@@ -176,6 +177,16 @@ struct DstirHandle {
     // adjoint of segment s runs on the caller's stream (double-buffered
     // segment states and grids, its own partial-sum buffer)
     int overlap = 1;            // option "overlap"
+    // option "persist": forward chains and the reverse pass's segments run as
+    // persistent cooperative launches (seg_fwd_kernel / seg_adj_kernel) with
+    // bounded grid barriers; "barrier_limit_us" bounds each wait, and
+    // "barrier_test" adds an arrival that never comes, so that every wait
+    // runs out (tests of the timeout path)
+    int persist = 0;
+    long long bar_limit_ns = 2000000000LL;
+    int bar_extra = 0;
+    GridBar* gbar = nullptr;
+    int seg_grid_max = -1;      // co-resident blocks of the persistent kernels (-1: not queried)
     cudaStream_t rstream = nullptr;
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_r[2] = {nullptr, nullptr}, ev_a[2] = {nullptr, nullptr};
     float* partial2 = nullptr;
@@ -373,6 +384,7 @@ void timed(DstirHandle* h, int kind, cudaStream_t st, Fn fn) {
         else if (kind == K_G2P) kind = K_G2P_RC;
         else if (kind == K_BIN) kind = K_BIN_RC;
         else if (kind == K_G2P_P2G) kind = K_G2P_P2G_RC;
+        else if (kind == K_SEG_FWD) kind = K_SEG_FWD_RC;
     }
     size_t i = h->prof.begin(kind, st);
     fn();
@@ -647,7 +659,7 @@ void dstir_destroy(DstirHandle* h) {
                     h->cnt, h->bkey, h->brank, h->bsum, h->cell_start, h->perm, h->fbuf, h->dfbuf, h->dpbuf,
                     h->bricks, h->rs_cnt, h->rs_start, h->rs_bsum, h->rs_key, h->rs_rank, h->rs_sorted,
                     h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0, h->box, h->vord, h->rs_vdest,
-                    h->partial2};
+                    h->partial2, h->gbar};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -714,6 +726,54 @@ bool fused_adj(const DstirHandle* h) { return h->fuse_adj && !binned(h); }
 const int* vorder_slot(const DstirHandle* h, int k, bool per_step);
 void enqueue_vorder(DstirHandle* h, const float* state, int* order, cudaStream_t st);
 
+// The persistent path: per-particle vector-RED scatter (p2g 1) in 256-thread
+// blocks, no fusion, no processing order, no binning.
+bool persist_on(const DstirHandle* h) {
+    return h->persist && h->p2g_variant == P2G_VEC && h->block == 256 && !h->fuse && !h->fuse_adj &&
+           h->reorder == 0 && h->gbar && h->seg_grid_max > 0;
+}
+
+int seg_grid(const DstirHandle* h) {
+    return std::max(1, std::min(h->seg_grid_max, std::max(h->n_blocks, h->n_gblocks + h->B)));
+}
+
+// A forward chain as persistent launches of up to kSegMax substeps.  Slots
+// that the grid update does not clear (clear_pm 0) are zeroed first.
+template <class SlotFn, class GridFn>
+void seg_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids, float* force, long long fstride,
+                 int fo0, int clear_pm, int box0, cudaStream_t st) {
+    for (int k0 = 0; k0 < nsteps; k0 += kSegMax) {
+        const int L = std::min(kSegMax, nsteps - k0);
+        SegFwdArgs g;
+        memset(&g, 0, sizeof(g));
+        for (int k = 0; k < L; ++k) {
+            float4 *pm, *vo;
+            grids(k0 + k, pm, vo);
+            if (!clear_pm) cudaMemsetAsync(pm, 0, (size_t)h->G * sizeof(float4), st);
+            g.cur[k] = slot(k0 + k);
+            g.next[k] = slot(k0 + k + 1);
+            g.pm[k] = pm;
+            g.vo[k] = vo;
+            g.box[k] = box_slot(h, box0 + k0 + k);
+        }
+        g.a = fwd_args(h, g.cur[0], g.next[0], g.pm[0], g.vo[0], t0 + k0, force, fstride, fo0 + k0, clear_pm);
+        g.a.n_gblocks = h->n_gblocks;
+        g.a.pdl = 0;
+        g.nsteps = L;
+        g.f0 = t0 + k0;
+        g.fo0 = fo0 + k0;
+        g.n_pblocks = h->n_blocks;
+        g.bar = h->gbar;
+        g.limit_ns = h->bar_limit_ns;
+        g.bar_extra = h->bar_extra;
+        // a launch that stopped at a barrier may leave a group counter of the
+        // block reductions behind; every launch starts from clear counters
+        cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), st);
+        cudaMemsetAsync(h->counters, 0, (size_t)3 * h->B * sizeof(unsigned), st);
+        timed(h, K_SEG_FWD, st, [&] { launch_seg_fwd(g, seg_grid(h), h->any_svd, st); });
+    }
+}
+
 // Forward chain of `nsteps` substeps over the state slots slot(0..nsteps).
 // With fusion: P2G(0), then per substep k the grid update and G2P(k) fused
 // with P2G(k+1); the last substep ends with a plain G2P unless `skip_last_g2p`.
@@ -735,6 +795,10 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
         grids(k, pm, vo);
         cudaMemsetAsync(pm, 0, (size_t)h->G * sizeof(float4), st);
     };
+    if (!fused(h) && persist_on(h)) {
+        seg_forward(h, t0, nsteps, slot, grids, force, fstride, fo0, clear_pm, box0, st);
+        return;
+    }
     if (!fused(h)) {
         for (int k = 0; k < nsteps; ++k) {
             float4 *pm, *vo;
@@ -1069,7 +1133,7 @@ namespace {
 // Enqueue the reverse pass of the recorded rollout.  dL/dforce is read from
 // h->dfbuf ([B][max_steps][3], entry fo = substep - t0); dL/dparams goes to
 // h->dpbuf.  Returns the adjoint slot holding dL/d(step-0 state).
-bool overlap_on(const DstirHandle* h) { return h->overlap && !binned(h) && !vorder_on(h); }
+bool overlap_on(const DstirHandle* h) { return h->overlap && !binned(h) && !vorder_on(h) && !persist_on(h); }
 
 int enqueue_backward(DstirHandle* h, cudaStream_t st) {
     const int n = h->rec_n, K = h->rec_K, t0 = h->rec_t0;
@@ -1161,7 +1225,37 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.lstage = h->lstage;
             return a;
         };
-        if (!fused_adj(h)) {
+        if (persist_on(h)) {
+            // substeps L-1 .. 0 in launches of up to kSegMax
+            for (int k1 = L - 1; k1 >= 0; k1 -= kSegMax) {
+                const int nq = std::min(kSegMax, k1 + 1);
+                SegAdjArgs g;
+                memset(&g, 0, sizeof(g));
+                for (int q = 0; q < nq; ++q) {
+                    const AdjArgs ak = adj_args(k1 - q);
+                    g.cur[q] = ak.cur;
+                    g.pm[q] = ak.pm;
+                    g.vo[q] = ak.vo;
+                    g.adj_next[q] = ak.adj_next;
+                    g.adj_cur[q] = ak.adj_cur;
+                    g.box[q] = ak.box;
+                }
+                g.a = adj_args(k1);
+                g.a.pdl = 0;
+                g.nsteps = nq;
+                g.f0 = t0 + s0 + k1;
+                g.fo0 = s0 + k1;
+                g.n_pblocks = h->n_blocks;
+                g.n_gblocks = h->n_gblocks;
+                g.bar = h->gbar;
+                g.status = h->status;
+                g.limit_ns = h->bar_limit_ns;
+                g.bar_extra = h->bar_extra;
+                cudaMemsetAsync(h->gbar, 0, sizeof(GridBar), s);
+                cudaMemsetAsync(h->counters, 0, (size_t)3 * h->B * sizeof(unsigned), s);
+                timed(h, K_SEG_ADJ, s, [&] { launch_seg_adj(g, seg_grid(h), h->any_svd, s); });
+            }
+        } else if (!fused_adj(h)) {
             for (int k = L - 1; k >= 0; --k) run_adj_substep(h, adj_args(k), s, k);
         } else {
             // G2P adjoint of the segment's last substep, then per substep k the
@@ -1340,6 +1434,27 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         h->overlap = value ? 1 : 0;
         return DSTIR_OK;
     }
+    if (!strcmp(key, "persist")) {
+        if (value && h->seg_grid_max < 0) h->seg_grid_max = seg_max_blocks(h->any_svd);
+        if (value && h->seg_grid_max <= 0)
+            return fail(h, DSTIR_EINVAL, "persist: cooperative launches are not available on this device");
+        int rc;
+        if (value && !h->gbar && (rc = dalloc(h, &h->gbar, 1, "grid barrier"))) return rc;
+        h->persist = value ? 1 : 0;
+        ++h->epoch;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "barrier_limit_us")) {
+        if (value < 1 || value > 60000000) return fail(h, DSTIR_EINVAL, "barrier_limit_us must be 1..60000000");
+        h->bar_limit_ns = value * 1000;
+        ++h->epoch;
+        return DSTIR_OK;
+    }
+    if (!strcmp(key, "barrier_test")) {
+        h->bar_extra = value ? 1 : 0;
+        ++h->epoch;
+        return DSTIR_OK;
+    }
     if (!strcmp(key, "lsort")) {
         h->lsort = value ? 1 : 0;
         return DSTIR_OK;
@@ -1431,6 +1546,10 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "reorder")) *value = h->reorder;
     else if (!strcmp(key, "store_grids")) *value = h->store_grids;
     else if (!strcmp(key, "overlap")) *value = h->overlap;
+    else if (!strcmp(key, "persist")) *value = h->persist;
+    else if (!strcmp(key, "persist_active")) *value = persist_on(h) ? 1 : 0;
+    else if (!strcmp(key, "barrier_limit_us")) *value = h->bar_limit_ns / 1000;
+    else if (!strcmp(key, "barrier_test")) *value = h->bar_extra;
     else if (!strcmp(key, "lsort")) *value = h->lsort;
     else if (!strcmp(key, "pdl")) *value = h->pdl;
     else if (!strcmp(key, "lstage")) *value = h->lstage;

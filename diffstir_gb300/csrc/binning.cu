@@ -819,7 +819,7 @@ __global__ void __launch_bounds__(256) g2p_brick_kernel(FwdArgs a, const BrickIn
     if (any_nan) atomicOr(a.status, DSTIR_STATUS_NAN);
     if (s.rod_mode == DSTIR_ROD_PARTICLES && s.n_rod > 0) {
         group_sum<3>(dv, sh, a.partial, a.counters + a.batch + br.scene, blockIdx.x - br.idx, br.count,
-                     a.force + br.scene * a.force_stride + (long long)a.fo * 3, s.force_scale);
+                     a.force + br.scene * a.force_stride + (long long)a.fo * 3, s.force_scale, blockIdx.x);
     }
 }
 
@@ -905,7 +905,7 @@ __global__ void __launch_bounds__(256) p2g_adj_brick_kernel(AdjArgs a, const Bri
         p2g_adj_finish<SVDJ>(a, s, prm, model, p, kind, m, Ab, vvb, fxb, pg);
     }
     group_sum<4>(pg, sh, a.partial, a.counters + 2 * a.batch + br.scene, blockIdx.x - br.idx, br.count,
-                 a.pgrad + ((long long)a.fo * a.batch + br.scene) * 4, 1.f);
+                 a.pgrad + ((long long)a.fo * a.batch + br.scene) * 4, 1.f, blockIdx.x);
 }
 
 void launch_g2p_brick(const FwdArgs& a, const BrickInfo* bricks, int n_bricks, const int* cell_start,

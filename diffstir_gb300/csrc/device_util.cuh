@@ -40,15 +40,17 @@ __device__ __forceinline__ void block_reduce(float (&v)[NV], float (*sh)[4]) {
 
 // Every block of a (scene, purpose) group publishes its partial sum; the block
 // that arrives last adds the partials of the group in block order (so the
-// result does not depend on scheduling) and writes it to out[0..NV).
+// result does not depend on scheduling) and writes it to out[0..NV).  `slot`
+// is the block's partial-sum slot (its block index, or its virtual block
+// index in a persistent kernel); the group's slots are group_first onwards.
 template <int NV>
 __device__ __forceinline__ void group_sum(float (&v)[NV], float (*sh)[4], float* partial, unsigned* counter,
-                                          int group_first, int group_count, float* out, float scale) {
+                                          int group_first, int group_count, float* out, float scale, int slot) {
     __shared__ bool is_last;
     block_reduce<NV>(v, sh);
     if (threadIdx.x == 0) {
 #pragma unroll
-        for (int c = 0; c < NV; ++c) partial[(long long)blockIdx.x * 4 + c] = v[c];
+        for (int c = 0; c < NV; ++c) partial[(long long)slot * 4 + c] = v[c];
         __threadfence();
         unsigned prev = atomicAdd(counter, 1u);
         is_last = (prev == (unsigned)(group_count - 1));
@@ -350,14 +352,28 @@ __device__ __forceinline__ bool box_inside(const int* box, int i, int j, int k) 
 
 // ---------------------------------------------------------------------------
 // state loads
+//
+// Load policy NC.  The one-substep kernels read their inputs through the
+// non-coherent read-only path (ld.global.nc), which is valid only for memory
+// that no thread writes while the kernel runs.  The persistent segment
+// kernels write, in one phase, what later phases read (states, grids,
+// adjoints), so they use plain loads (NC false); the acquire side of their
+// grid barrier makes the other blocks' writes visible to those.
 // ---------------------------------------------------------------------------
+template <bool NC, class T>
+__device__ __forceinline__ T ldp(const T* p) {
+    if constexpr (NC) return __ldg(p);
+    else return *p;
+}
+template <bool NC = true>
 __device__ __forceinline__ void load3(const float* st, long long stride, int o, long long p, float* v) {
 #pragma unroll
-    for (int c = 0; c < 3; ++c) v[c] = __ldg(st + (long long)(o + c) * stride + p);
+    for (int c = 0; c < 3; ++c) v[c] = ldp<NC>(st + (long long)(o + c) * stride + p);
 }
+template <bool NC = true>
 __device__ __forceinline__ void load9(const float* st, long long stride, int o, long long p, float* v) {
 #pragma unroll
-    for (int c = 0; c < 9; ++c) v[c] = __ldg(st + (long long)(o + c) * stride + p);
+    for (int c = 0; c < 9; ++c) v[c] = ldp<NC>(st + (long long)(o + c) * stride + p);
 }
 __device__ __forceinline__ void store3(float* st, long long stride, int o, long long p, const float* v) {
 #pragma unroll

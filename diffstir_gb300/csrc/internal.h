@@ -191,6 +191,64 @@ void launch_unpermute(const float* in, float* out, const int* dest, long long st
                       cudaStream_t st);
 void launch_reduce_pgrad(const float* pgrad, int T, int B, float* out, cudaStream_t s);
 
+// ---------------------------------------------------------------------------
+// Persistent segment kernels (option "persist"): one cooperative launch runs
+// up to kSegMax substeps of a forward chain, or of a segment's reverse pass,
+// with grid-wide barriers between the phases of a substep, instead of one
+// launch per phase.  For small scenes, whose substeps are bound by launch
+// latency rather than by the GPU's bandwidth.
+// ---------------------------------------------------------------------------
+constexpr int kSegMax = 50;
+
+// State of the grid barrier, zeroed before every launch.  A block that waits
+// longer than the launch's limit sets DSTIR_STATUS_TIMEOUT and `abort`; every
+// block then leaves the kernel at its next barrier.
+struct GridBar {
+    unsigned count;   // arrivals in the current generation
+    unsigned gen;     // generation, advanced by the last arrival
+    unsigned abort;   // set when a wait ran past the limit
+    unsigned pad;
+};
+
+struct SegFwdArgs {
+    FwdArgs a;                    // fields shared by the substeps; cur, next, pm, vo, box, f, fo set per substep
+    const float* cur[kSegMax];    // state read by substep k
+    float* next[kSegMax];         // state written by substep k
+    float4* pm[kSegMax];
+    float4* vo[kSegMax];
+    int* box[kSegMax];
+    int nsteps;                   // substeps of this launch (<= kSegMax)
+    int f0, fo0;                  // substep k uses trajectory index f0 + k and force entry fo0 + k
+    int n_pblocks;                // particle blocks (the blk table)
+    GridBar* bar;
+    long long limit_ns;           // longest wait at a barrier
+    int bar_extra;                // arrivals a barrier waits for beyond the grid's blocks (0; tests: 1)
+};
+
+struct SegAdjArgs {
+    AdjArgs a;                    // fields shared by the substeps; the arrays below set the rest
+    const float* cur[kSegMax];    // entry q: the q-th substep of the launch (substeps descending)
+    const float4* pm[kSegMax];
+    const float4* vo[kSegMax];
+    const float* adj_next[kSegMax];
+    float* adj_cur[kSegMax];
+    const int* box[kSegMax];
+    int nsteps;
+    int f0, fo0;                  // entry q is substep f0 - q, force entry fo0 - q
+    int n_pblocks;
+    int n_gblocks;
+    GridBar* bar;
+    unsigned* status;             // DSTIR_STATUS_* word (the adjoint kernels have none of their own)
+    long long limit_ns;
+    int bar_extra;
+};
+
+// Largest co-resident grid of the persistent kernels (blocks of 256 threads),
+// 0 when they cannot be launched cooperatively on this device.
+int seg_max_blocks(bool svdj);
+cudaError_t launch_seg_fwd(const SegFwdArgs& g, int grid, bool svdj, cudaStream_t st);
+cudaError_t launch_seg_adj(const SegAdjArgs& g, int grid, bool svdj, cudaStream_t st);
+
 void launch_svd3(const float* A, float* U, float* S, float* V, long long n, cudaStream_t s);
 void launch_svd3_backward(const float* gU, const float* gS, const float* gV, const float* U, const float* S,
                           const float* V, float* gA, long long n, cudaStream_t s);

@@ -25,14 +25,18 @@ namespace dstir {
 // ---------------------------------------------------------------------------
 // forward
 // ---------------------------------------------------------------------------
-template <int VARIANT, bool SVDJ, int MINB>
-__global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
-    pdl_enter();
+// The kernel bodies below take their block index `vb` as an argument: a
+// one-substep kernel passes blockIdx.x, a persistent segment kernel loops its
+// blocks over the virtual blocks of each phase (every body ends with no
+// pending barrier, and the caller separates two bodies by __syncthreads).
+// NC: load policy (ldp in device_util.cuh).
+template <int VARIANT, bool SVDJ, bool NC>
+__device__ __forceinline__ void p2g_body(const FwdArgs& a, int vb) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ int boxsh[8][6];
     if (threadIdx.x == 0) {
-        bi = a.blk[blockIdx.x];
+        bi = a.blk[vb];
         s = a.sc[bi.scene];
     }
     __syncthreads();
@@ -54,7 +58,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
             staged = (a.lstage & 1) && blockDim.x <= 256;
             if (staged && (int)threadIdx.x < count)
 #pragma unroll
-                for (int c = 0; c < NS; ++c) pst[c][threadIdx.x] = __ldg(a.cur + (long long)c * a.stride + p);
+                for (int c = 0; c < NS; ++c) pst[c][threadIdx.x] = ldp<NC>(a.cur + (long long)c * a.stride + p);
             // local_interleave's barriers make the staged state visible
             slot = local_interleave_any(a.cur, a.stride, bi.start, count, s.inv_dx, s.n, lo);
             p = bi.start + slot;
@@ -75,9 +79,9 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
 #pragma unroll
         for (int i = 0; i < 9; ++i) C[i] = pst[OC + i][slot];
     } else {
-        load3(a.cur, a.stride, OX, p, x);
-        load3(a.cur, a.stride, OV, p, v);
-        load9(a.cur, a.stride, OC, p, C);
+        load3<NC>(a.cur, a.stride, OX, p, x);
+        load3<NC>(a.cur, a.stride, OV, p, v);
+        load9<NC>(a.cur, a.stride, OC, p, C);
     }
     float m, vv[3], A[9];
     if (bi.kind == KIND_LIQUID) {
@@ -86,7 +90,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
 #pragma unroll
             for (int i = 0; i < 9; ++i) F[i] = pst[OF + i][slot];
         } else {
-            load9(a.cur, a.stride, OF, p, F);
+            load9<NC>(a.cur, a.stride, OF, p, F);
         }
 #pragma unroll
         for (int i = 0; i < 4; ++i) prm[i] = __ldg(a.params + bi.scene * 4 + i);
@@ -112,7 +116,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
         for (int c = 0; c < 3; ++c) vv[c] = q.vv[c];
     } else {
         float F[9];
-        load9(a.cur, a.stride, OF, p, F);
+        load9<NC>(a.cur, a.stride, OF, p, F);
         if (active) store9(a.next, a.stride, OF, p, F);
         m = (bi.kind == KIND_ROD) ? s.m_rod : s.m_cont;
 #pragma unroll
@@ -178,6 +182,12 @@ __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
         }
 }
 
+template <int VARIANT, bool SVDJ, int MINB>
+__global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
+    pdl_enter();
+    p2g_body<VARIANT, SVDJ, true>(a, blockIdx.x);
+}
+
 // Reaction force of the moving cylinder (the rod branch of grid_op
 // :212-220 summed as compute_loss :330-336 does for the rod particles), run
 // by the extra blocks of grid_kernel, one per scene: the block walks the nodes
@@ -234,18 +244,22 @@ __device__ __forceinline__ void rod_force_block(const FwdArgs& a, int scene, Sce
         for (int c = 0; c < 3; ++c) a.force[scene * a.force_stride + (long long)a.fo * 3 + c] = fsum[c];
 }
 
-__global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
-    pdl_enter();
+// Grid update of the nodes of virtual block vb, or the rod force of one scene
+// for vb >= n_gblocks.  LOOP: the block's threads loop over the node block's
+// nodes (a persistent kernel, whose blocks may be smaller than the node
+// blocks); otherwise one thread per node.
+template <bool LOOP>
+__device__ __forceinline__ void grid_body(const FwdArgs& a, int vb) {
     __shared__ SceneDev s;
     __shared__ float rc[3], rc1[3];
     __shared__ float sh[32][4];
-    if ((int)blockIdx.x >= a.n_gblocks) {  // block-uniform: a rod-force block
-        rod_force_block(a, (int)blockIdx.x - a.n_gblocks, s, sh);
+    if (vb >= a.n_gblocks) {  // block-uniform: a rod-force block
+        rod_force_block(a, vb - a.n_gblocks, s, sh);
         return;
     }
     // every thread reads the block descriptor (one broadcast load), so the
     // scene copy and the trajectory loads do not wait on a serial chain
-    const GridBlock gb = a.gblk[blockIdx.x];
+    const GridBlock gb = a.gblk[vb];
     load_scene_shared(s, a.sc + gb.scene);
     if (threadIdx.x < 3) {
         const float* t0 = a.traj + ((long long)gb.scene * a.traj_len + a.f) * 3;
@@ -253,57 +267,67 @@ __global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
         rc1[threadIdx.x] = t0[3 + threadIdx.x];
     }
     __syncthreads();
-    long long node = gb.start + threadIdx.x;
     const int n = s.n;
-    int i, j, k;
-    node_ijk((int)(node - s.goff), n, i, j, k);
-    // nodes outside the occupied box hold no mass and no stencil reads them:
-    // their P2G entry is still zero and their velocity is never gathered
-    if (node < gb.end && (!a.box || box_inside(a.box + gb.scene * 6, i, j, k))) {
-        float4 g = a.pm[node];
-        // nodes inside the rod belong to the rod-force block, which reads
-        // and clears their P2G entries (their velocity is the rod's anyway)
-        const bool in_rod = s.rod_mode == DSTIR_ROD_CYLINDER && in_rod_cylinder(s, rc, i, j, k);
-        if (a.clear_pm && !in_rod) a.pm[node] = make_float4(0.f, 0.f, 0.f, 0.f);
-        float inv_m = 1.f / (g.w + 1e-10f);
-        float v[3] = {inv_m * g.x, inv_m * g.y, inv_m * g.z};
-        if (s.container_wall) {  // :204-210
-            float d0 = (float)i * s.dx - s.ccx, d2 = (float)k * s.dx - s.ccz;
-            float n2 = d0 * d0 + d2 * d2;
-            if (n2 > s.cr2) {
-                float inv = 1.f / sqrtf(n2);
-                float u0 = d0 * inv, u2 = d2 * inv;
-                float dot = v[0] * u0 + v[2] * u2;
-                v[0] -= u0 * dot;
-                v[2] -= u2 * dot;
+    auto node_fn = [&](long long node) {
+        int i, j, k;
+        node_ijk((int)(node - s.goff), n, i, j, k);
+        // nodes outside the occupied box hold no mass and no stencil reads them:
+        // their P2G entry is still zero and their velocity is never gathered
+        if (!a.box || box_inside(a.box + gb.scene * 6, i, j, k)) {
+            float4 g = a.pm[node];
+            // nodes inside the rod belong to the rod-force block, which reads
+            // and clears their P2G entries (their velocity is the rod's anyway)
+            const bool in_rod = s.rod_mode == DSTIR_ROD_CYLINDER && in_rod_cylinder(s, rc, i, j, k);
+            if (a.clear_pm && !in_rod) a.pm[node] = make_float4(0.f, 0.f, 0.f, 0.f);
+            float inv_m = 1.f / (g.w + 1e-10f);
+            float v[3] = {inv_m * g.x, inv_m * g.y, inv_m * g.z};
+            if (s.container_wall) {  // :204-210
+                float d0 = (float)i * s.dx - s.ccx, d2 = (float)k * s.dx - s.ccz;
+                float n2 = d0 * d0 + d2 * d2;
+                if (n2 > s.cr2) {
+                    float inv = 1.f / sqrtf(n2);
+                    float u0 = d0 * inv, u2 = d2 * inv;
+                    float dot = v[0] * u0 + v[2] * u2;
+                    v[0] -= u0 * dot;
+                    v[2] -= u2 * dot;
+                }
             }
-        }
-        int b = s.bound;  // :211-224
-        if (i < b && v[0] < 0.f) v[0] = 0.f;
-        if (i > n - b && v[0] > 0.f) v[0] = 0.f;
-        if (k < b && v[2] < 0.f) v[2] = 0.f;
-        if (k > n - b && v[2] > 0.f) v[2] = 0.f;
-        if (j < b && v[1] < 0.f) v[1] = 0.f;
-        if (j > n - b && v[1] > 0.f) v[0] = v[1] = v[2] = 0.f;
-        if (in_rod)
+            int b = s.bound;  // :211-224
+            if (i < b && v[0] < 0.f) v[0] = 0.f;
+            if (i > n - b && v[0] > 0.f) v[0] = 0.f;
+            if (k < b && v[2] < 0.f) v[2] = 0.f;
+            if (k > n - b && v[2] > 0.f) v[2] = 0.f;
+            if (j < b && v[1] < 0.f) v[1] = 0.f;
+            if (j > n - b && v[1] > 0.f) v[0] = v[1] = v[2] = 0.f;
+            if (in_rod)
 #pragma unroll
-            for (int c = 0; c < 3; ++c) v[c] = (rc1[c] - rc[c]) / s.dt;
-        a.vo[node] = make_float4(v[0], v[1], v[2], 0.f);
+                for (int c = 0; c < 3; ++c) v[c] = (rc1[c] - rc[c]) / s.dt;
+            a.vo[node] = make_float4(v[0], v[1], v[2], 0.f);
+        }
+    };
+    if (LOOP) {
+        for (long long node = gb.start + threadIdx.x; node < gb.end; node += blockDim.x) node_fn(node);
+    } else if (gb.start + threadIdx.x < gb.end) {
+        node_fn(gb.start + threadIdx.x);
     }
+}
+
+__global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
+    pdl_enter();
+    grid_body<false>(a, blockIdx.x);
 }
 
 // WRITE_F: also write F of the next state, F_tmp = (I + dt C) F of the
 // current one (what P2G stores, :39-42, :153), for the reverse pass's state
 // recompute when the P2G grids of the rollout were kept and P2G is not rerun.
-template <int MINB, bool WRITE_F>
-__global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
-    pdl_enter();
+template <bool WRITE_F, bool NC>
+__device__ __forceinline__ void g2p_body(const FwdArgs& a, int vb) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
     __shared__ float tv[3];
     if (threadIdx.x == 0) {
-        bi = a.blk[blockIdx.x];
+        bi = a.blk[vb];
         s = a.sc[bi.scene];
         const float* t0 = a.traj + ((long long)bi.scene * a.traj_len + a.f) * 3;
         for (int c = 0; c < 3; ++c) tv[c] = (t0[3 + c] - t0[c]) / s.dt;
@@ -315,7 +339,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
     if (active) {
         if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
         float x[3];
-        load3(a.cur, a.stride, OX, p, x);
+        load3<NC>(a.cur, a.stride, OX, p, x);
         int base[3];
         float fx[3];
         float nv[3] = {0.f, 0.f, 0.f};
@@ -335,7 +359,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
                     float wij = w[i][0] * w[j][1];
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
-                        float4 g = __ldg(a.vo + row + k);
+                        float4 g = ldp<NC>(a.vo + row + k);
                         float W = wij * w[k][2];
                         float wg[3] = {W * g.x, W * g.y, W * g.z};
 #pragma unroll
@@ -357,8 +381,8 @@ __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
         }
         if (WRITE_F) {
             float Cc[9], F[9], Ft[9];
-            load9(a.cur, a.stride, OC, p, Cc);
-            load9(a.cur, a.stride, OF, p, F);
+            load9<NC>(a.cur, a.stride, OC, p, Cc);
+            load9<NC>(a.cur, a.stride, OF, p, F);
             if (bi.kind == KIND_LIQUID) {
                 float IC[9];
 #pragma unroll
@@ -401,9 +425,15 @@ __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
         store3(a.next, a.stride, OX, p, nx);
     }
     if (bi.kind == KIND_ROD && s.rod_mode == DSTIR_ROD_PARTICLES) {
-        group_sum<3>(dv, sh, a.partial, a.counters + a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,
-                     a.force + bi.scene * a.force_stride + (long long)a.fo * 3, s.force_scale);
+        group_sum<3>(dv, sh, a.partial, a.counters + a.batch + bi.scene, vb - bi.idx, bi.count,
+                     a.force + bi.scene * a.force_stride + (long long)a.fo * 3, s.force_scale, vb);
     }
+}
+
+template <int MINB, bool WRITE_F>
+__global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
+    pdl_enter();
+    g2p_body<WRITE_F, true>(a, blockIdx.x);
 }
 
 // G2P of substep f fused with P2G of substep f+1 (one thread per particle).
@@ -583,21 +613,20 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
     }
     if (bi.kind == KIND_ROD && s.rod_mode == DSTIR_ROD_PARTICLES) {
         group_sum<3>(dv, sh, a.partial, a.counters + a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,
-                     a.force + bi.scene * a.force_stride + (long long)a.fo * 3, s.force_scale);
+                     a.force + bi.scene * a.force_stride + (long long)a.fo * 3, s.force_scale, blockIdx.x);
     }
 }
 
 // ---------------------------------------------------------------------------
 // adjoint
 // ---------------------------------------------------------------------------
-template <int VARIANT, int MINB>
-__global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
-    pdl_enter();
+template <int VARIANT, bool NC>
+__device__ __forceinline__ void g2p_adj_body(const AdjArgs& a, int vb) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float fb[3];
     if (threadIdx.x == 0) {
-        bi = a.blk[blockIdx.x];
+        bi = a.blk[vb];
         s = a.sc[bi.scene];
         const float* d = a.dforce + bi.scene * a.dforce_stride + (long long)a.fo * 3;
         for (int c = 0; c < 3; ++c) fb[c] = d[c];
@@ -623,7 +652,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
             staged = (a.lstage & 2) && blockDim.x <= 256;
             if (staged && (int)threadIdx.x < count) {
 #pragma unroll
-                for (int c = 0; c < 3; ++c) ast[c][threadIdx.x] = __ldg(a.cur + (long long)(OX + c) * a.stride + p);
+                for (int c = 0; c < 3; ++c) ast[c][threadIdx.x] = ldp<NC>(a.cur + (long long)(OX + c) * a.stride + p);
 #pragma unroll
                 for (int c = 0; c < 15; ++c) ast[3 + c][threadIdx.x] = a.adj_next[(long long)c * a.stride + p];
             }
@@ -645,8 +674,8 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
 #pragma unroll
         for (int i = 0; i < 9; ++i) Cb[i] = ast[3 + OC + i][slot];
     } else {
-        load3(a.cur, a.stride, OX, p, x);
-        load9(a.adj_next, a.stride, OC, p, Cb);
+        load3<NC>(a.cur, a.stride, OX, p, x);
+        load9<NC>(a.adj_next, a.stride, OC, p, Cb);
     }
     if (bi.kind == KIND_LIQUID) {
         float ax[3], av[3];
@@ -657,8 +686,8 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
                 av[c] = ast[3 + OV + c][slot];
             }
         } else {
-            load3(a.adj_next, a.stride, OX, p, ax);
-            load3(a.adj_next, a.stride, OV, p, av);
+            load3<NC>(a.adj_next, a.stride, OX, p, ax);
+            load3<NC>(a.adj_next, a.stride, OV, p, av);
         }
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
@@ -723,7 +752,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
                         cw[k] = make_float4(g0, g1, g2, 0.f);
                     }
                     if (liquid) {
-                        const float4 g = __ldg(a.vo + row + k);
+                        const float4 g = ldp<NC>(a.vo + row + k);
                         const float Wb = g.x * rk0 + g.y * rk1 + g.z * rk2;
                         U[0] += W * g.x;
                         U[1] += W * g.y;
@@ -755,11 +784,18 @@ __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
     }
 }
 
-__global__ void __launch_bounds__(1024) grid_adj_kernel(AdjArgs a) {
+template <int VARIANT, int MINB>
+__global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
     pdl_enter();
+    g2p_adj_body<VARIANT, true>(a, blockIdx.x);
+}
+
+// Grid adjoint of the nodes of virtual block vb (LOOP: see grid_body).
+template <bool LOOP>
+__device__ __forceinline__ void grid_adj_body(const AdjArgs& a, int vb) {
     __shared__ SceneDev s;
     __shared__ float rc[3], rodv[3], fb[3];
-    const GridBlock gb = a.gblk[blockIdx.x];
+    const GridBlock gb = a.gblk[vb];
     load_scene_shared(s, a.sc + gb.scene);
     __syncthreads();
     if (threadIdx.x < 3) {
@@ -771,79 +807,88 @@ __global__ void __launch_bounds__(1024) grid_adj_kernel(AdjArgs a) {
         fb[c] = d[c];
     }
     __syncthreads();
-    long long node = gb.start + threadIdx.x;
-    if (node >= gb.end) return;
     const int n = s.n;
-    int i, j, k;
-    node_ijk((int)(node - s.goff), n, i, j, k);
-    // outside the occupied box the velocity adjoint is zero (no stencil
-    // scattered there) and no stencil gathers the P/M adjoint
-    if (a.box && !box_inside(a.box + gb.scene * 6, i, j, k)) return;
-    float4 g = a.pm[node];
-    float4 vb4 = a.ga[node];
-    a.ga[node] = make_float4(0.f, 0.f, 0.f, 0.f);
-    float inv_m = 1.f / (g.w + 1e-10f);
-    float u[3] = {inv_m * g.x, inv_m * g.y, inv_m * g.z};
-    float v[3] = {u[0], u[1], u[2]};
-    bool proj = false;
-    float u0 = 0.f, u2 = 0.f;
-    if (s.container_wall) {
-        float d0 = (float)i * s.dx - s.ccx, d2 = (float)k * s.dx - s.ccz;
-        float n2 = d0 * d0 + d2 * d2;
-        if (n2 > s.cr2) {
-            float inv = 1.f / sqrtf(n2);
-            u0 = d0 * inv;
-            u2 = d2 * inv;
-            float dot = v[0] * u0 + v[2] * u2;
-            v[0] -= u0 * dot;
-            v[2] -= u2 * dot;
-            proj = true;
+    auto node_fn = [&](long long node) {
+        int i, j, k;
+        node_ijk((int)(node - s.goff), n, i, j, k);
+        // outside the occupied box the velocity adjoint is zero (no stencil
+        // scattered there) and no stencil gathers the P/M adjoint
+        if (a.box && !box_inside(a.box + gb.scene * 6, i, j, k)) return;
+        float4 g = a.pm[node];
+        float4 vb4 = a.ga[node];
+        a.ga[node] = make_float4(0.f, 0.f, 0.f, 0.f);
+        float inv_m = 1.f / (g.w + 1e-10f);
+        float u[3] = {inv_m * g.x, inv_m * g.y, inv_m * g.z};
+        float v[3] = {u[0], u[1], u[2]};
+        bool proj = false;
+        float u0 = 0.f, u2 = 0.f;
+        if (s.container_wall) {
+            float d0 = (float)i * s.dx - s.ccx, d2 = (float)k * s.dx - s.ccz;
+            float n2 = d0 * d0 + d2 * d2;
+            if (n2 > s.cr2) {
+                float inv = 1.f / sqrtf(n2);
+                u0 = d0 * inv;
+                u2 = d2 * inv;
+                float dot = v[0] * u0 + v[2] * u2;
+                v[0] -= u0 * dot;
+                v[2] -= u2 * dot;
+                proj = true;
+            }
         }
-    }
-    float mask[3] = {1.f, 1.f, 1.f};
-    int b = s.bound;
-    if (i < b && v[0] < 0.f) { v[0] = 0.f; mask[0] = 0.f; }
-    if (i > n - b && v[0] > 0.f) { v[0] = 0.f; mask[0] = 0.f; }
-    if (k < b && v[2] < 0.f) { v[2] = 0.f; mask[2] = 0.f; }
-    if (k > n - b && v[2] > 0.f) { v[2] = 0.f; mask[2] = 0.f; }
-    if (j < b && v[1] < 0.f) { v[1] = 0.f; mask[1] = 0.f; }
-    if (j > n - b && v[1] > 0.f) { mask[0] = mask[1] = mask[2] = 0.f; }
-    bool inside = false;
-    if (s.rod_mode == DSTIR_ROD_CYLINDER) {
-        inside = in_rod_cylinder(s, rc, i, j, k);  // the forward's classification
-    }
-    float ub[3], mb = 0.f;
-    if (inside) {
+        float mask[3] = {1.f, 1.f, 1.f};
+        int b = s.bound;
+        if (i < b && v[0] < 0.f) { v[0] = 0.f; mask[0] = 0.f; }
+        if (i > n - b && v[0] > 0.f) { v[0] = 0.f; mask[0] = 0.f; }
+        if (k < b && v[2] < 0.f) { v[2] = 0.f; mask[2] = 0.f; }
+        if (k > n - b && v[2] > 0.f) { v[2] = 0.f; mask[2] = 0.f; }
+        if (j < b && v[1] < 0.f) { v[1] = 0.f; mask[1] = 0.f; }
+        if (j > n - b && v[1] > 0.f) { mask[0] = mask[1] = mask[2] = 0.f; }
+        bool inside = false;
+        if (s.rod_mode == DSTIR_ROD_CYLINDER) {
+            inside = in_rod_cylinder(s, rc, i, j, k);  // the forward's classification
+        }
+        float ub[3], mb = 0.f;
+        if (inside) {
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
-            ub[c] = -g.w * fb[c] / s.dt;
-            mb += fb[c] * (rodv[c] - u[c]) / s.dt;
+            for (int c = 0; c < 3; ++c) {
+                ub[c] = -g.w * fb[c] / s.dt;
+                mb += fb[c] * (rodv[c] - u[c]) / s.dt;
+            }
+        } else {
+            ub[0] = mask[0] * vb4.x;
+            ub[1] = mask[1] * vb4.y;
+            ub[2] = mask[2] * vb4.z;
+            if (proj) {
+                float dot = ub[0] * u0 + ub[2] * u2;
+                ub[0] -= u0 * dot;
+                ub[2] -= u2 * dot;
+            }
         }
-    } else {
-        ub[0] = mask[0] * vb4.x;
-        ub[1] = mask[1] * vb4.y;
-        ub[2] = mask[2] * vb4.z;
-        if (proj) {
-            float dot = ub[0] * u0 + ub[2] * u2;
-            ub[0] -= u0 * dot;
-            ub[2] -= u2 * dot;
-        }
+        float Pu = g.x * ub[0] + g.y * ub[1] + g.z * ub[2];
+        a.pmb[node] = make_float4(inv_m * ub[0], inv_m * ub[1], inv_m * ub[2], mb - inv_m * inv_m * Pu);
+    };
+    if (LOOP) {
+        for (long long node = gb.start + threadIdx.x; node < gb.end; node += blockDim.x) node_fn(node);
+    } else if (gb.start + threadIdx.x < gb.end) {
+        node_fn(gb.start + threadIdx.x);
     }
-    float Pu = g.x * ub[0] + g.y * ub[1] + g.z * ub[2];
-    a.pmb[node] = make_float4(inv_m * ub[0], inv_m * ub[1], inv_m * ub[2], mb - inv_m * inv_m * Pu);
+}
+
+__global__ void __launch_bounds__(1024) grid_adj_kernel(AdjArgs a) {
+    pdl_enter();
+    grid_adj_body<false>(a, blockIdx.x);
 }
 
 // P2G adjoint, one thread per particle (pieces in adjoint.cuh).
-template <bool SVDJ, int MINB>
-__global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
-    pdl_enter();
+template <bool SVDJ, bool NC>
+__device__ __forceinline__ void p2g_adj_body(const AdjArgs& a, int vb) {
     __shared__ SceneDev s;
     __shared__ BlockInfo bi;
     __shared__ float sh[32][4];
     __shared__ float prm[4];
     __shared__ int model;
     if (threadIdx.x == 0) {
-        bi = a.blk[blockIdx.x];
+        bi = a.blk[vb];
         s = a.sc[bi.scene];
         for (int i = 0; i < 4; ++i) prm[i] = a.params[bi.scene * 4 + i];
         model = a.models[bi.scene];
@@ -855,9 +900,9 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
         const bool liquid = bi.kind == KIND_LIQUID;
         if (a.order && liquid) p = a.order[p];
         float x[3];
-        load3(a.cur, a.stride, OX, p, x);
+        load3<NC>(a.cur, a.stride, OX, p, x);
         float m, mv[3], A[9];
-        p2g_adj_affine<SVDJ>(a.cur, a.stride, s, prm, model, p, bi.kind, m, mv, A);
+        p2g_adj_affine<SVDJ, NC>(a.cur, a.stride, s, prm, model, p, bi.kind, m, mv, A);
         float Ab[9], vvb[3] = {0.f, 0.f, 0.f}, fxb[3] = {0.f, 0.f, 0.f};
 #pragma unroll
         for (int i = 0; i < 9; ++i) Ab[i] = 0.f;
@@ -866,14 +911,20 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
         if (locate(x, s.inv_dx, s.n, base, fx)) {
             float w[3][3], dw[3][3];
             bspline_d(fx, w, dw);
-            p2g_adj_gather(a.pmb, s, base, fx, w, dw, m, mv, A, liquid, Ab, vvb, fxb);
+            p2g_adj_gather<NC>(a.pmb, s, base, fx, w, dw, m, mv, A, liquid, Ab, vvb, fxb);
         }
-        p2g_adj_finish<SVDJ>(a, s, prm, model, p, bi.kind, m, Ab, vvb, fxb, pg);
+        p2g_adj_finish<SVDJ, NC>(a, s, prm, model, p, bi.kind, m, Ab, vvb, fxb, pg);
     }
     if (bi.kind == KIND_LIQUID) {
-        group_sum<4>(pg, sh, a.partial, a.counters + 2 * a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,
-                     a.pgrad + ((long long)a.fo * a.batch + bi.scene) * 4, 1.f);
+        group_sum<4>(pg, sh, a.partial, a.counters + 2 * a.batch + bi.scene, vb - bi.idx, bi.count,
+                     a.pgrad + ((long long)a.fo * a.batch + bi.scene) * 4, 1.f, vb);
     }
+}
+
+template <bool SVDJ, int MINB>
+__global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
+    pdl_enter();
+    p2g_adj_body<SVDJ, true>(a, blockIdx.x);
 }
 
 // P2G adjoint of substep f fused with the G2P adjoint of substep f-1.  The
@@ -1021,7 +1072,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_g2p_adj_kernel(AdjArgs a) {
     }
     if (bi.kind == KIND_LIQUID) {
         group_sum<4>(pg, sh, a.partial, a.counters + 2 * a.batch + bi.scene, blockIdx.x - bi.idx, bi.count,
-                     a.pgrad + ((long long)a.fo * a.batch + bi.scene) * 4, 1.f);
+                     a.pgrad + ((long long)a.fo * a.batch + bi.scene) * 4, 1.f, blockIdx.x);
     }
 }
 
@@ -1074,6 +1125,183 @@ __global__ void reduce_pgrad_kernel(const float* pgrad, int T, int B, float* out
     for (int t = threadIdx.x; t < T; t += blockDim.x) acc[0] += pgrad[((long long)t * B + b) * 4 + c];
     block_reduce<1>(acc, sh);
     if (threadIdx.x == 0) out[b * 4 + c] = acc[0];
+}
+
+// ---------------------------------------------------------------------------
+// persistent segment kernels
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ unsigned long long global_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+__device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// Grid-wide barrier of a cooperative launch (all blocks co-resident).  Thread
+// 0 of each block publishes the block's writes (fence), arrives, and the last
+// arrival opens the next generation with a release store; the others wait for
+// it with acquire loads, which also make the other blocks' writes visible to
+// the plain loads after the barrier.  The wait is bounded: past `limit_ns`
+// the block raises DSTIR_STATUS_TIMEOUT and `abort`, and a block that sees
+// `abort` stops waiting too.  Returns false, for the whole block, when the
+// kernel must end.  `expected`: arrivals that open the barrier (the grid's
+// blocks, plus one in the test that makes every wait run out).
+__device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned expected, long long limit_ns, unsigned* status) {
+    __shared__ int go;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int ok = 1;
+        const unsigned gen = ld_acquire_gpu(&b->gen);
+        __threadfence();
+        const unsigned arrived = atomicAdd(&b->count, 1u) + 1u;
+        if (arrived == expected) {
+            b->count = 0u;  // ordered before the release of the next generation
+            st_release_gpu(&b->gen, gen + 1u);
+        } else {
+            const unsigned long long t0 = global_ns();
+            while (ld_acquire_gpu(&b->gen) == gen) {
+                if (ld_acquire_gpu(&b->abort)) {
+                    ok = 0;
+                    break;
+                }
+                if ((long long)(global_ns() - t0) > limit_ns) {
+                    atomicOr(status, DSTIR_STATUS_TIMEOUT);
+                    atomicExch(&b->abort, 1u);
+                    ok = 0;
+                    break;
+                }
+                __nanosleep(100);
+            }
+        }
+        go = ok;
+    }
+    __syncthreads();
+    return go != 0;
+}
+
+// A chain of forward substeps in one launch.  Per substep: P2G over the
+// particle blocks, barrier, grid update over the node blocks and the rod-force
+// blocks, barrier, G2P over the particle blocks.  Block b always takes the
+// particle blocks b, b + gridDim.x, ..., so the state G2P writes is read by
+// the same block's P2G of the next substep, and no barrier is needed between
+// them; the grid update of the next substep comes after the next P2G
+// barrier, by which time every block has finished its G2P reads of the
+// velocity grid.  The P2G grid of each substep must start at zero (the grid
+// update clears it with clear_pm, or the caller zeroed every slot).
+template <bool SVDJ>
+__global__ void __launch_bounds__(256, 2) seg_fwd_kernel(SegFwdArgs g) {
+    const unsigned expected = gridDim.x + (unsigned)g.bar_extra;
+    const int nvb_grid = g.a.n_gblocks + g.a.batch;
+    for (int k = 0; k < g.nsteps; ++k) {
+        FwdArgs a = g.a;
+        a.cur = g.cur[k];
+        a.next = g.next[k];
+        a.pm = g.pm[k];
+        a.vo = g.vo[k];
+        a.box = g.box[k];
+        a.f = g.f0 + k;
+        a.fo = g.fo0 + k;
+        for (int vb = blockIdx.x; vb < g.n_pblocks; vb += gridDim.x) {
+            p2g_body<P2G_VEC, SVDJ, false>(a, vb);
+            __syncthreads();
+        }
+        if (!grid_barrier(g.bar, expected, g.limit_ns, a.status)) return;
+        for (int vb = blockIdx.x; vb < nvb_grid; vb += gridDim.x) {
+            grid_body<true>(a, vb);
+            __syncthreads();
+        }
+        if (!grid_barrier(g.bar, expected, g.limit_ns, a.status)) return;
+        for (int vb = blockIdx.x; vb < g.n_pblocks; vb += gridDim.x) {
+            g2p_body<false, false>(a, vb);
+            __syncthreads();
+        }
+    }
+}
+
+// The reverse pass of up to kSegMax substeps (descending) in one launch.  Per
+// substep: G2P adjoint (scatter into the grid adjoint), barrier, grid adjoint
+// (clears the grid adjoint, writes the P/M adjoint), barrier, P2G adjoint
+// (gathers the P/M adjoint).  As in seg_fwd_kernel a block keeps its particle
+// blocks, so the state adjoint the P2G adjoint writes is read by the same
+// block's G2P adjoint of the substep before; the next grid adjoint rewrites
+// the P/M adjoint only after the next G2P-adjoint barrier, when every block
+// has finished gathering it.
+template <bool SVDJ>
+__global__ void __launch_bounds__(256, 2) seg_adj_kernel(SegAdjArgs g) {
+    const unsigned expected = gridDim.x + (unsigned)g.bar_extra;
+    for (int q = 0; q < g.nsteps; ++q) {
+        AdjArgs a = g.a;
+        a.cur = g.cur[q];
+        a.pm = g.pm[q];
+        a.vo = g.vo[q];
+        a.adj_next = g.adj_next[q];
+        a.adj_cur = g.adj_cur[q];
+        a.box = g.box[q];
+        a.f = g.f0 - q;
+        a.fo = g.fo0 - q;
+        for (int vb = blockIdx.x; vb < g.n_pblocks; vb += gridDim.x) {
+            g2p_adj_body<P2G_VEC, false>(a, vb);
+            __syncthreads();
+        }
+        if (!grid_barrier(g.bar, expected, g.limit_ns, g.status)) return;
+        for (int vb = blockIdx.x; vb < g.n_gblocks; vb += gridDim.x) {
+            grid_adj_body<true>(a, vb);
+            __syncthreads();
+        }
+        if (!grid_barrier(g.bar, expected, g.limit_ns, g.status)) return;
+        for (int vb = blockIdx.x; vb < g.n_pblocks; vb += gridDim.x) {
+            p2g_adj_body<SVDJ, false>(a, vb);
+            __syncthreads();
+        }
+    }
+}
+
+int seg_max_blocks(bool svdj) {
+    int dev = 0, sms = 0, coop = 0, f = 0, a = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 0;
+    if (cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, dev) != cudaSuccess || !coop) return 0;
+    if (svdj) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, seg_fwd_kernel<true>, 256, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, seg_adj_kernel<true>, 256, 0) != cudaSuccess)
+            return 0;
+    } else {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&f, seg_fwd_kernel<false>, 256, 0) != cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, seg_adj_kernel<false>, 256, 0) != cudaSuccess)
+            return 0;
+    }
+    return sms * (f < a ? f : a);
+}
+
+template <class Args>
+cudaError_t coop_launch(void (*k)(Args), int grid, cudaStream_t st, const Args& g) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)grid);
+    cfg.blockDim = dim3(256);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = st;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, k, g);
+}
+
+cudaError_t launch_seg_fwd(const SegFwdArgs& g, int grid, bool svdj, cudaStream_t st) {
+    if (g.nsteps <= 0) return cudaSuccess;
+    return svdj ? coop_launch(seg_fwd_kernel<true>, grid, st, g) : coop_launch(seg_fwd_kernel<false>, grid, st, g);
+}
+cudaError_t launch_seg_adj(const SegAdjArgs& g, int grid, bool svdj, cudaStream_t st) {
+    if (g.nsteps <= 0) return cudaSuccess;
+    return svdj ? coop_launch(seg_adj_kernel<true>, grid, st, g) : coop_launch(seg_adj_kernel<false>, grid, st, g);
 }
 
 // ---------------------------------------------------------------------------

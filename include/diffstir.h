@@ -41,6 +41,8 @@ extern "C" {
 /* bits of the device status word (dstir_status) */
 #define DSTIR_STATUS_NAN 1u          /* a non-finite particle state was produced */
 #define DSTIR_STATUS_OUT_OF_GRID 2u  /* a particle stencil left the grid; it was skipped */
+#define DSTIR_STATUS_TIMEOUT 4u      /* a grid barrier of a persistent launch waited past its limit;
+                                        the launch stopped early and its results are void */
 
 /* viscosity models: src/simulator/simulation_functions.py:118-146 */
 #define DSTIR_MODEL_CARREAU 0   /* params [eta0, eta_inf, n, lambda] */
@@ -178,7 +180,17 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * previous kernel of the stream drains and wait in hardware for its
  * completion before touching memory; 1 in forward rollouts, 2 also in the
  * reverse pass, 0 never), "brick_scatter" /
- * "brick_gather" (scatter and gather forms of variant 3), "profile" [0] (1:
+ * "brick_gather" (scatter and gather forms of variant 3), "persist" [0] (1:
+ * with p2g 1, 256-thread particle blocks and no fusion or processing order,
+ * each chunk of a forward rollout and each segment of the reverse pass runs
+ * as cooperative launches of up to 50 substeps, the phases of a substep
+ * separated by grid-wide barriers, instead of one launch per phase; for
+ * scenes too small to fill the GPU; the reverse pass then runs on one
+ * stream), "barrier_limit_us" [2000000] (longest wait at a grid barrier of a
+ * persistent launch; past it the launch stops early and raises
+ * DSTIR_STATUS_TIMEOUT), "barrier_test" [0] (1: every grid barrier waits for
+ * one arrival more than the launch has blocks, so that every wait runs out;
+ * for tests of the timeout path), "profile" [0] (1:
  * time every launch with CUDA events; totals via dstir_get_option
  * "prof_ns:<kernel>" / "prof_count:<kernel>"), "launches" (reset the launch
  * counter). */

@@ -96,6 +96,18 @@ def scene_record(sf):
     return rec
 
 
+STATE_KEYS = ('x', 'v', 'C', 'F', 'operator_x', 'operator_C', 'container_C')
+
+
+def subsample_states(out, stride):
+    """Keep the per-frame particle states of frames 0, stride, 2 stride, ...
+    only (forces, losses and gradients stay complete); records the stride."""
+    for key in list(out):
+        if key[:1] == 'm' and key.split('_', 1)[-1] in STATE_KEYS:
+            out[key] = out[key][::stride]
+    out['meta_state_stride'] = np.int64(stride)
+
+
 def run_fixture(ref_root, name, n_grid, n_liq, n_op, n_cont, T, seed, prec, models,
                 with_grad, out_dir, extra=None):
     """``extra`` (optional): 'dt' replaces simulation_setting.dt, 'scene'
@@ -171,6 +183,8 @@ def run_fixture(ref_root, name, n_grid, n_liq, n_op, n_cont, T, seed, prec, mode
             out[p + 'grad_C1'] = sf.C.grad.to_numpy()[1] if sf.max_steps > 1 else np.zeros(0)
         print('%s model %d: %.1fs loss=%r' % (name, model, time.time() - t0,
                                                float(out[p + 'loss'])), flush=True)
+    if 'state_stride' in extra:
+        subsample_states(out, extra['state_stride'])
     out['meta_config'] = np.array(json.dumps(cfg))
     out['meta_prec'] = np.array(prec)
     out['meta_seed'] = np.int64(seed)
@@ -186,7 +200,7 @@ def run_fixture(ref_root, name, n_grid, n_liq, n_op, n_cont, T, seed, prec, mode
 # clamps :211-220 and the sticky top :221-224) and the rod dv (:266-270)
 # accumulates over many frames.  Trajectory rounded to multiples of 2^-24.
 LONG = {'scene': {'container_diameter': 0.74, 'liquid_height': 0.58, 'container_height': 0.6},
-        'traj_quantum': 2.0 ** -24}
+        'traj_quantum': 2.0 ** -24, 'state_stride': 10}
 
 FIXTURES = {
     # name: (n_grid, n_liquid, n_rod, n_container, substeps T, seed, precision, models, grad[, extra])

@@ -74,32 +74,62 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 4, 'store_grids': 1, 'graph': 1, 'reorder': 3}, {'p2g': 4, 'lsort': 0},
             {'p2g': 4, 'block': 128}, {'p2g': 4, 'block': 64, 'graph': 1}, {'p2g': 4, 'pdl': 0},
             {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 4, 'pdl': 2, 'graph': 1},
-            {'p2g': 4, 'lstage': 0}, {'p2g': 4, 'graph': 1, 'block': 128, 'tight': 2}, {'p2g': 4, 'graph': 0}]
+            {'p2g': 4, 'lstage': 0}, {'p2g': 4, 'graph': 1, 'block': 128, 'tight': 2}, {'p2g': 4, 'graph': 0},
+            {'p2g': 1, 'persist': 1, 'graph': 0}, {'p2g': 1, 'persist': 1, 'graph': 1}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
                'warp-tight0', 'warp-tight1', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph', 'warp-store',
                'warp-store-graph-reorder3', 'warp-nolsort', 'warp-block128', 'warp-block64-graph', 'warp-nopdl',
-               'warp-fused-graph', 'warp-pdl2-graph', 'warp-nostage', 'warp-graph-block128-tight2', 'warp-eager']
+               'warp-fused-graph', 'warp-pdl2-graph', 'warp-nostage', 'warp-graph-block128-tight2', 'warp-eager',
+               'vec-persist', 'vec-persist-graph']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
 @pytest.mark.parametrize('model', [0, 1, 2])
 def test_reference_scene_golden(model, opts):
-    """Reference scene (container, rod particles, k=20000) built by the
-    reference's own code: GPU vs the FP64 oracle and vs the reference's
-    compute_loss gradient."""
+    """The reference's scene (container, rod particles, k=20000) as the
+    reference's own code built and ran it for 60 substeps, in a wide, tall
+    container whose fluid meets every wall clamp, the sticky top and the
+    container projection (tests/golden/make_golden.py, fixture
+    ref_f64_g16_long).  The GPU is compared directly with the reference's own
+    results: its rod force profile (compute_loss, simulation_functions.py
+    :330-339) within 1e-4 and the gradient of its L1 loss that ti.ad.Tape
+    produced (gradient_descent_module.py:103-107) within 1e-3, given the same
+    dL/dforce; and with the FP64 oracle on the same inputs.  The fixture's
+    trajectory is exactly representable in float32, so the rod velocity
+    (q[f+1]-q[f])/dt is the same on both sides."""
+    sc, d = fixture_scene('ref_f64_g16_long', model)
+    T = sc.n_steps
+    p = 'm%d_' % model
+    ref_force = d[p + 'total_operator_dv'] * sc.desc.force_scale   # entry f+1 is the GPU's entry f
+    loss, dF = gu.reference_loss_and_dforce(ref_force[1:], d[p + 'target'], T)
+    assert abs(loss - float(d[p + "loss"])) <= 1e-10 * abs(loss)
+    force_g, dp_g, _, st = gpu_force_and_grad(sc, T, dF, ckpt=25, options=opts)
+    assert st == 0
+    assert rel(force_g[:T - 1], ref_force[1:T]) < FORCE_RTOL
+    assert rel(dp_g, d[p + 'grad_params']) < GRAD_RTOL, (dp_g, d[p + 'grad_params'])
+    scr = rounded(sc)
+    force_o, dp_o, _ = oracle_force_and_grad(scr, T, dF)
+    assert rel(force_g, force_o) < FORCE_RTOL
+    assert rel(dp_g, dp_o) < GRAD_RTOL, (dp_g, dp_o)
+
+
+@pytest.mark.parametrize('model', [0, 1, 2])
+def test_reference_scene_golden_g32(model):
+    """The 32^3 fixture (6 substeps): GPU against the FP64 oracle on
+    float32-rounded inputs.  Its trajectory is not float32-exact, so the
+    direct comparison with the reference's own numbers is the oracle's
+    (tests/test_oracle_golden.py), not this one's."""
     sc, d = fixture_scene('ref_f64_g32', model)
     sc = rounded(sc)
     T = sc.n_steps
     force_o, _, _ = oracle.rollout(sc.desc, sc.params, sc.trajectory, T, sc.x0())
     loss, dF = gu.reference_loss_and_dforce(force_o, d['m%d_target' % model], T)
-    force_g, dp_g, _, st = gpu_force_and_grad(sc, T, dF, options=opts)
+    force_g, dp_g, _, st = gpu_force_and_grad(sc, T, dF)
     assert st == 0
     _, dp_o, _ = oracle_force_and_grad(sc, T, dF)
     assert rel(force_g, force_o) < FORCE_RTOL
     assert rel(dp_g, dp_o) < GRAD_RTOL, (dp_g, dp_o)
-    # and against the reference's own (float64) gradient, whose trajectory was not rounded
-    assert rel(dp_g, d['m%d_grad_params' % model]) < 5e-2
 
 
 @pytest.mark.parametrize('model,params', [(S.MODEL_HB, (0.5, 0.3, 0.7, 0.0)),
