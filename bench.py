@@ -254,38 +254,6 @@ def cpu_sample(sc, T_sample, threads):
     return time.perf_counter() - t0
 
 
-def oracle_segments(desc, p, traj, T, x0, K, threads, w=None):
-    """FP64 oracle rollout of T substeps chained over K-substep segments (the
-    oracle keeps every state of a call, so long rollouts of large scenes run
-    segment by segment).  Without ``w``: returns the forces [T,3].  With ``w``
-    = dL/dforce [T,3]: also runs the reverse pass segment by segment, last to
-    first, each seeded with the state adjoint the later segment produced, and
-    returns (forces, dL/dparams[4])."""
-    import oracle
-    N = x0.shape[0]
-    state = np.zeros((N, 24))
-    state[:, 0:3] = x0
-    state[:, 15:24] = np.eye(3).reshape(1, 9)
-    starts, ckpts, forces = list(range(0, T, K)), [], []
-    for s0 in starts:
-        L = min(K, T - s0)
-        ckpts.append(state)
-        f, state, rc = oracle.rollout_last(desc, p, traj[s0:s0 + L + 1], L, state[:, 0:3], state[:, 3:6],
-                                           state[:, 6:15], state[:, 15:24], threads=threads)
-        forces.append(f)
-    force = np.concatenate(forces, 0)
-    if w is None:
-        return force
-    dp = np.zeros(4)
-    seed = None
-    for s0, st in reversed(list(zip(starts, ckpts))):
-        L = min(K, T - s0)
-        _, dps, seed, _ = oracle.grad_seeded(desc, p, traj[s0:s0 + L + 1], L, st[:, 0:3], w[s0:s0 + L], seed,
-                                             st[:, 3:6], st[:, 6:15], st[:, 15:24], threads=threads)
-        dp += dps
-    return force, dp
-
-
 def fp64_grad_check(sc, p32, target32, Ts, norm, gpu_dp, free, names, h_rel, threads, K=50):
     """The GPU adjoint of scene 0's force loss over the first Ts substeps
     against the FP64 oracle: its adjoint (the reverse pass of the oracle's
@@ -302,10 +270,11 @@ def fp64_grad_check(sc, p32, target32, Ts, norm, gpu_dp, free, names, h_rel, thr
         d = (force - tgt)[:, 0::2]
         return float((d * d).sum() / norm)
 
-    f64 = oracle_segments(desc, p, traj, Ts, x0, K, threads)
+    import oracle
+    f64 = oracle.rollout_chain(desc, p, traj, Ts, x0, K, threads)
     w = np.zeros((Ts, 3))
     w[:, 0::2] = 2.0 * (f64 - tgt)[:, 0::2] / norm
-    _, dp64 = oracle_segments(desc, p, traj, Ts, x0, K, threads, w)
+    _, dp64 = oracle.rollout_chain(desc, p, traj, Ts, x0, K, threads, w)
     out = {'what': 'GPU adjoint (FP32) of scene 0 against the FP64 oracle over the first %d substeps: the '
                    'oracle\'s own reverse pass, and its central differences at h = %g x |param|' % (Ts, h_rel),
            'substeps': Ts, 'threads': threads, 'gpu_adjoint': {}, 'fp64_adjoint': {}, 'fp64_fd': {},
@@ -315,8 +284,8 @@ def fp64_grad_check(sc, p32, target32, Ts, norm, gpu_dp, free, names, h_rel, thr
         pp, pm = p.copy(), p.copy()
         pp[i] += h
         pm[i] -= h
-        fd = (loss_of(oracle_segments(desc, pp, traj, Ts, x0, K, threads)) -
-              loss_of(oracle_segments(desc, pm, traj, Ts, x0, K, threads))) / (2.0 * h)
+        fd = (loss_of(oracle.rollout_chain(desc, pp, traj, Ts, x0, K, threads)) -
+              loss_of(oracle.rollout_chain(desc, pm, traj, Ts, x0, K, threads))) / (2.0 * h)
         g, a = float(gpu_dp[i]), float(dp64[i])
         nm = names[i]
         out['gpu_adjoint'][nm], out['fp64_adjoint'][nm], out['fp64_fd'][nm] = g, a, fd

@@ -39,6 +39,13 @@ CANDIDATES = [
     {'p2g': 3, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 256, 'graph': 0, 'brick_scatter': 2,
      'brick_gather': 0},
 ]
+# persistent cooperative launches: tried for scenes that fill less than half
+# of the GPU's 256-particle block slots at one block per SM, where launch
+# latency rather than bandwidth bounds a substep
+PERSIST_CANDIDATES = [
+    {'p2g': 1, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 256, 'graph': 1, 'tight': 1, 'persist': 1},
+]
+PERSIST_MAX_PARTICLES = 76 * 256
 
 
 def cache_path():
@@ -56,7 +63,7 @@ def shape_key(scenes):
     rod = scenes[0].desc.rod_mode
     svd = int(any(s.desc.j_mode == 1 for s in scenes))
     name = torch.cuda.get_device_name() if torch.cuda.is_available() else 'cpu'
-    return 'v11|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
+    return 'v12|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
 
 
 def _load():
@@ -114,7 +121,11 @@ def autotune(scenes, nsteps=200, ckpt=50, candidates=None, use_cache=True, verbo
     nsteps = max(1, min(nsteps, max(s.n_steps for s in lst)))
     ckpt = min(ckpt, nsteps)
     results = []
-    for opt in (candidates or CANDIDATES):
+    if candidates is None:
+        candidates = list(CANDIDATES)
+        if sum(s.n_particles for s in lst) <= PERSIST_MAX_PARTICLES:
+            candidates += PERSIST_CANDIDATES
+    for opt in candidates:
         t0 = time.perf_counter()
         try:
             t = time_config(scenes, opt, nsteps, ckpt)

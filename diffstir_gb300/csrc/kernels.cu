@@ -1140,25 +1140,31 @@ __device__ __forceinline__ unsigned ld_acquire_gpu(const unsigned* p) {
     asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
     return v;
 }
+__device__ __forceinline__ unsigned ld_relaxed_gpu(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.relaxed.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 __device__ __forceinline__ void st_release_gpu(unsigned* p, unsigned v) {
     asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
 // Grid-wide barrier of a cooperative launch (all blocks co-resident).  Thread
 // 0 of each block publishes the block's writes (fence), arrives, and the last
-// arrival opens the next generation with a release store; the others wait for
-// it with acquire loads, which also make the other blocks' writes visible to
-// the plain loads after the barrier.  The wait is bounded: past `limit_ns`
-// the block raises DSTIR_STATUS_TIMEOUT and `abort`, and a block that sees
-// `abort` stops waiting too.  Returns false, for the whole block, when the
-// kernel must end.  `expected`: arrivals that open the barrier (the grid's
-// blocks, plus one in the test that makes every wait run out).
+// arrival opens the next generation with a release store; the others poll the
+// generation with relaxed loads and, once it moved, take one acquire fence,
+// which makes the other blocks' writes visible to the plain loads after the
+// barrier.  The wait is bounded: past `limit_ns` the block raises
+// DSTIR_STATUS_TIMEOUT and `abort`, and a block that sees `abort` stops
+// waiting too.  Returns false, for the whole block, when the kernel must end.
+// `expected`: arrivals that open the barrier (the grid's blocks, plus one in
+// the test that makes every wait run out).
 __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned expected, long long limit_ns, unsigned* status) {
     __shared__ int go;
     __syncthreads();
     if (threadIdx.x == 0) {
         int ok = 1;
-        const unsigned gen = ld_acquire_gpu(&b->gen);
+        const unsigned gen = ld_relaxed_gpu(&b->gen);
         __threadfence();
         const unsigned arrived = atomicAdd(&b->count, 1u) + 1u;
         if (arrived == expected) {
@@ -1166,20 +1172,23 @@ __device__ __forceinline__ bool grid_barrier(GridBar* b, unsigned expected, long
             st_release_gpu(&b->gen, gen + 1u);
         } else {
             const unsigned long long t0 = global_ns();
-            while (ld_acquire_gpu(&b->gen) == gen) {
-                if (ld_acquire_gpu(&b->abort)) {
-                    ok = 0;
-                    break;
+            unsigned spins = 0;
+            while (ld_relaxed_gpu(&b->gen) == gen) {
+                if ((++spins & 63u) == 0u) {
+                    if (ld_relaxed_gpu(&b->abort)) {
+                        ok = 0;
+                        break;
+                    }
+                    if ((long long)(global_ns() - t0) > limit_ns) {
+                        atomicOr(status, DSTIR_STATUS_TIMEOUT);
+                        atomicExch(&b->abort, 1u);
+                        ok = 0;
+                        break;
+                    }
                 }
-                if ((long long)(global_ns() - t0) > limit_ns) {
-                    atomicOr(status, DSTIR_STATUS_TIMEOUT);
-                    atomicExch(&b->abort, 1u);
-                    ok = 0;
-                    break;
-                }
-                __nanosleep(100);
             }
         }
+        __threadfence();  // acquire: the writes released before the generation moved
         go = ok;
     }
     __syncthreads();

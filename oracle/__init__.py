@@ -164,6 +164,40 @@ def grad_seeded(desc, params, traj, T, x0, dL_dforce, dL_dstateT=None, v0=None, 
     return force, dp, ds, rc
 
 
+def rollout_chain(desc, params, traj, T, x0, K, threads=1, w=None):
+    """FP64 rollout of T substeps from rest at positions x0, chained over
+    K-substep segments through :func:`rollout_last` (a call keeps every state
+    of its substeps, so long rollouts of large scenes run segment by segment).
+    Without ``w``: returns the forces [T,3].  With ``w`` = dL/dforce [T,3]:
+    also runs the reverse pass segment by segment, last to first, each seeded
+    with the state adjoint of the later segment (:func:`grad_seeded`), and
+    returns (forces, dL/dparams[4])."""
+    x0 = np.asarray(x0, np.float64)
+    N = x0.shape[0]
+    state = np.zeros((N, 24))
+    state[:, 0:3] = x0
+    state[:, 15:24] = np.eye(3).reshape(1, 9)
+    starts, ckpts, forces = list(range(0, T, K)), [], []
+    for s0 in starts:
+        L = min(K, T - s0)
+        ckpts.append(state)
+        f, state, _ = rollout_last(desc, params, traj[s0:s0 + L + 1], L, state[:, 0:3], state[:, 3:6],
+                                   state[:, 6:15], state[:, 15:24], threads=threads)
+        forces.append(f)
+    force = np.concatenate(forces, 0)
+    if w is None:
+        return force
+    w = np.asarray(w, np.float64).reshape(T, 3)
+    dp = np.zeros(4)
+    seed = None
+    for s0, st in reversed(list(zip(starts, ckpts))):
+        L = min(K, T - s0)
+        _, dps, seed, _ = grad_seeded(desc, params, traj[s0:s0 + L + 1], L, st[:, 0:3], w[s0:s0 + L], seed,
+                                      st[:, 3:6], st[:, 6:15], st[:, 15:24], threads=threads)
+        dp += dps
+    return force, dp
+
+
 def svd3(A):
     lib = load()
     A = _arr(A).reshape(-1, 9)

@@ -101,7 +101,9 @@ def test_reference_scene_golden(model, opts):
     sc, d = fixture_scene('ref_f64_g16_long', model)
     T = sc.n_steps
     p = 'm%d_' % model
-    ref_force = d[p + 'total_operator_dv'] * sc.desc.force_scale   # entry f+1 is the GPU's entry f
+    # the reference's force (compute_loss :335-336, in float64); entry f+1 is the GPU's entry f
+    scale = float(d['scene_operator_p_vol']) * float(d['scene_operator_density']) / float(d['scene_dt'])
+    ref_force = d[p + 'total_operator_dv'] * scale
     loss, dF = gu.reference_loss_and_dforce(ref_force[1:], d[p + 'target'], T)
     assert abs(loss - float(d[p + "loss"])) <= 1e-10 * abs(loss)
     force_g, dp_g, _, st = gpu_force_and_grad(sc, T, dF, ckpt=25, options=opts)
