@@ -70,7 +70,8 @@ def parse():
     ap.add_argument('--substeps', type=int, default=None, help='override the substep count')
     ap.add_argument('--ckpt', type=int, default=None)
     ap.add_argument('--batch', type=int, default=None, help='scenes per GPU (default: the configuration\'s)')
-    ap.add_argument('--p2g', type=int, default=None, help='0 scalar atomics, 1 vector atomics, 2 binned cells')
+    ap.add_argument('--p2g', type=int, default=None,
+                    help='0 scalar atomics, 1 vector atomics, 3 brick tiles, 4 warp-aggregated vector atomics')
     ap.add_argument('--graph', type=int, default=None, help='1: replay rollouts as CUDA graphs')
     ap.add_argument('--block', type=int, default=None)
     ap.add_argument('--gblock', type=int, default=None)
@@ -82,7 +83,6 @@ def parse():
     ap.add_argument('--resort', type=int, default=None, help='1: re-sort the particle order at every checkpoint')
     ap.add_argument('--tight', type=int, default=None, help='register-cap level of the particle kernels: 0, 1 or 2')
     ap.add_argument('--box', type=int, default=None, help='1: grid kernels skip nodes outside the occupied box')
-    ap.add_argument('--reorder', type=int, default=None, help='processing order rebuilt every N substeps (0: never)')
     ap.add_argument('--store-grids', type=int, default=None, help='1: keep every substep\'s grids, recompute states only')
     ap.add_argument('--overlap', type=int, default=None, help='1: segment recompute on a second stream')
     ap.add_argument('--lsort', type=int, default=None, help='1: re-interleave each block before the warp scatters')
@@ -460,7 +460,7 @@ def run_ours(args):
     sc = scenes[0]
     opts = {}
     keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather', 'fuse', 'fuse_adj', 'resort', 'tight',
-            'box', 'reorder', 'store_grids', 'overlap', 'lsort', 'pdl', 'lstage', 'persist')
+            'box', 'store_grids', 'overlap', 'lsort', 'pdl', 'lstage', 'persist')
     explicit = any(getattr(args, k) is not None for k in keys)
     if args.autotune and not explicit:
         from diffstir_gb300 import autotune
@@ -728,7 +728,7 @@ def run_ours(args):
 
     status_all = int(st) | int(sim.status())
     opts_used = {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather',
-                                                'fuse', 'fuse_adj', 'resort', 'tight', 'box', 'reorder',
+                                                'fuse', 'fuse_adj', 'resort', 'tight', 'box',
                                                 'store_grids', 'overlap', 'lsort', 'pdl', 'lstage', 'persist')}
     scatter_variant, scatter_fused = sim.get_option('p2g'), sim.get_option('fuse')
     sim.close()

@@ -145,8 +145,8 @@ struct DstirHandle {
     unsigned* status = nullptr;
     int* box = nullptr;              // [max_steps][B][6] occupied node box of each substep
 
-    // per-substep binning (p2g variant P2G_CELL); one (cell_start, perm) slot per
-    // substep of a segment, so the reverse pass reuses the recompute's bins
+    // per-substep binning (p2g variant P2G_BRICK); one (cell_start, perm) slot
+    // per substep of a segment, so the reverse pass reuses the recompute's bins
     int* cnt = nullptr;         // [G+1]
     int* bkey = nullptr;        // [stride]
     int* brank = nullptr;       // [stride]
@@ -167,7 +167,6 @@ struct DstirHandle {
     int resort = 1;             // option "resort": 0 never
     int tight = 2;              // option "tight": register-cap level of the particle kernels (0, 1, 2)
     int use_box = 1;            // option "box": the grid kernels skip nodes outside the occupied box
-    int reorder = 0;            // option "reorder": processing order rebuilt every this many substeps (0: never)
     int store_grids = 0;        // option "store_grids": a recorded rollout keeps every substep's grids
     int lsort = 1;              // option "lsort": warp-aggregated scatters re-interleave each block's particles
     int pdl = 1;                // option "pdl": programmatic dependent launch, 1 forward rollouts, 2 everywhere
@@ -191,9 +190,6 @@ struct DstirHandle {
     cudaEvent_t ev_fork = nullptr, ev_join = nullptr, ev_r[2] = {nullptr, nullptr}, ev_a[2] = {nullptr, nullptr};
     float* partial2 = nullptr;
     float* fwd_partial = nullptr;  // partial-sum buffer for the forward kernels being enqueued (NULL: partial)
-    int* vord = nullptr;        // [vord_slots][stride] processing orders (slot j: substeps [jR, (j+1)R) of a segment)
-    long long vord_slots = 0;
-    int* rs_vdest = nullptr;    // [stride] scratch of the processing-order build
     int max_n = 0;              // largest n_grid of the batch
     int* rs_cnt = nullptr;      // [G+1]
     int* rs_start = nullptr;    // [G+2]
@@ -408,7 +404,7 @@ int ensure_bin_slots(DstirHandle* h, long long n) {
     return DSTIR_OK;
 }
 
-bool binned(const DstirHandle* h) { return h->p2g_variant == P2G_CELL || h->p2g_variant == P2G_BRICK; }
+bool binned(const DstirHandle* h) { return h->p2g_variant == P2G_BRICK; }
 
 // Occupied-box slot of relative substep k (NULL for the binned variants,
 // whose scatter kernels do not track the box: their grid update covers every
@@ -426,11 +422,10 @@ void reset_boxes(DstirHandle* h, long long k0, long long n, cudaStream_t st) {
 int* slot_cell_start(DstirHandle* h, int slot) { return h->cell_start + (size_t)slot * (h->nbins_max + 2); }
 int* slot_perm(DstirHandle* h, int slot) { return h->perm + (size_t)slot * h->stride; }
 
-// One forward substep.  With the binned variant the particles of `a.cur` are
-// counting-sorted into bin slot `bin_slot` first.
+// One forward substep.  With the binned variant (bricks) the particles of
+// `a.cur` are counting-sorted into bin slot `bin_slot` first.
 void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot = 0) {
     if (binned(h)) {
-        const bool brick = h->p2g_variant == P2G_BRICK;
         BinArgs b;
         b.sc = h->sc;
         b.blk = h->blk;
@@ -442,20 +437,14 @@ void run_substep(DstirHandle* h, const FwdArgs& a, cudaStream_t st, int bin_slot
         b.cell_start = slot_cell_start(h, bin_slot);
         b.perm = slot_perm(h, bin_slot);
         b.bsum = h->bsum;
-        b.G = brick ? h->nbins_brick : h->G;
+        b.G = h->nbins_brick;
         b.status = h->status;
-        b.key_mode = brick ? 1 : 0;
+        b.key_mode = 1;
         h->launches += 4;
         timed(h, K_BIN, st, [&] { launch_bin(b, h->n_blocks, h->block, st); });
-        if (brick)
-            timed(h, K_P2G, st, [&] {
-                launch_p2g_brick(a, h->bricks, h->n_bricks, b.cell_start, b.perm, b.G, h->any_svd, h->brick_scatter,
-                                 st);
-            });
-        else
-            timed(h, K_P2G, st, [&] {
-                launch_p2g_cell(a, b.cell_start, b.perm, h->n_gblocks, h->gblock, h->G, h->any_svd, st);
-            });
+        timed(h, K_P2G, st, [&] {
+            launch_p2g_brick(a, h->bricks, h->n_bricks, b.cell_start, b.perm, b.G, h->any_svd, h->brick_scatter, st);
+        });
     } else {
         timed(h, K_P2G, st, [&] { launch_p2g(a, h->n_blocks, h->block, h->p2g_variant, h->any_svd, st, h->tight); });
     }
@@ -474,11 +463,6 @@ void run_adj_substep(DstirHandle* h, const AdjArgs& a, cudaStream_t st, int bin_
         timed(h, K_G2P_ADJ, st, [&] {
             launch_g2p_adj_brick(a, h->bricks, h->n_bricks, slot_cell_start(h, bin_slot), slot_perm(h, bin_slot),
                                  h->nbins_brick, h->brick_scatter, st);
-        });
-    } else if (h->p2g_variant == P2G_CELL) {
-        timed(h, K_G2P_ADJ, st, [&] {
-            launch_g2p_adj_cell(a, slot_cell_start(h, bin_slot), slot_perm(h, bin_slot), h->n_gblocks, h->gblock,
-                                h->G, st);
         });
     } else {
         const int var = h->p2g_variant;  // P2G_PLAIN, P2G_VEC or P2G_WARP here
@@ -658,8 +642,7 @@ void dstir_destroy(DstirHandle* h) {
                     h->traj, h->params, h->models, h->force_scratch, h->pgrad, h->partial, h->counters, h->status,
                     h->cnt, h->bkey, h->brank, h->bsum, h->cell_start, h->perm, h->fbuf, h->dfbuf, h->dpbuf,
                     h->bricks, h->rs_cnt, h->rs_start, h->rs_bsum, h->rs_key, h->rs_rank, h->rs_sorted,
-                    h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0, h->box, h->vord, h->rs_vdest,
-                    h->partial2, h->gbar};
+                    h->rs_dest, h->perm_cur, h->perm_tmp, h->perm_rec0, h->box, h->partial2, h->gbar};
     for (void* p : ptrs)
         if (p) cudaFree(p);
     delete h;
@@ -723,14 +706,12 @@ namespace {
 bool fused(const DstirHandle* h) { return h->fuse && !binned(h); }
 bool fused_adj(const DstirHandle* h) { return h->fuse_adj && !binned(h); }
 
-const int* vorder_slot(const DstirHandle* h, int k, bool per_step);
-void enqueue_vorder(DstirHandle* h, const float* state, int* order, cudaStream_t st);
 
 // The persistent path: per-particle vector-RED scatter (p2g 1) in 256-thread
 // blocks, no fusion, no processing order, no binning.
 bool persist_on(const DstirHandle* h) {
-    return h->persist && h->p2g_variant == P2G_VEC && h->block == 256 && !h->fuse && !h->fuse_adj &&
-           h->reorder == 0 && h->gbar && h->seg_grid_max > 0;
+    return h->persist && h->p2g_variant == P2G_VEC && h->block == 256 && !h->fuse && !h->fuse_adj && h->gbar &&
+           h->seg_grid_max > 0;
 }
 
 int seg_grid(const DstirHandle* h) {
@@ -806,10 +787,6 @@ void chain_forward(DstirHandle* h, int t0, int nsteps, SlotFn slot, GridFn grids
             zero_slot(k);
             FwdArgs a = fwd_args(h, slot(k), slot(k + 1), pm, vo, t0 + k, force, fstride, fo0 + k, clear_pm);
             a.box = box_slot(h, box0 + k);
-            // per_step_bins marks the segment recompute, whose orders the
-            // reverse pass reuses; a forward rollout keeps one order slot
-            a.order = vorder_slot(h, k, per_step_bins);
-            if (a.order && k % h->reorder == 0) enqueue_vorder(h, slot(k), const_cast<int*>(a.order), st);
             run_substep(h, a, st, per_step_bins ? k : 0);
         }
         return;
@@ -891,51 +868,6 @@ void enqueue_resort(DstirHandle* h, const float* in, float* out, int* dest, cuda
 // Number of re-sorts in a rollout of nsteps substeps, chunk length K.
 long long resort_count(const DstirHandle* h, int nsteps, int K) {
     return resort_on(h) && K > 0 && nsteps > K ? (nsteps - 1) / K : 0;
-}
-
-// The processing order is rebuilt every h->reorder substeps inside each chain
-// of the unfused per-particle path (the fused kernels run two substeps per
-// thread and keep the physical order).
-bool vorder_on(const DstirHandle* h) { return h->reorder > 0 && resort_on(h) && !fused(h) && !fused_adj(h); }
-
-int ensure_vorder(DstirHandle* h, int K) {
-    if (!vorder_on(h)) return DSTIR_OK;
-    int rc;
-    if ((rc = ensure_resort(h, 1))) return rc;
-    if (!h->rs_vdest && (rc = dalloc(h, &h->rs_vdest, (size_t)h->stride, "processing-order scratch"))) return rc;
-    long long slots = std::max<long long>(1, (K - 1) / h->reorder + 1);
-    if (slots > h->vord_slots) {
-        if ((rc = dalloc(h, &h->vord, (size_t)(slots * h->stride), "processing orders"))) return rc;
-        h->vord_slots = slots;
-    }
-    return DSTIR_OK;
-}
-
-// Processing order of substep k of a chain: NULL before the first rebuild.
-const int* vorder_slot(const DstirHandle* h, int k, bool per_step) {
-    if (!vorder_on(h) || k < h->reorder) return nullptr;
-    return h->vord + (size_t)(per_step ? k / h->reorder : 0) * h->stride;
-}
-
-void enqueue_vorder(DstirHandle* h, const float* state, int* order, cudaStream_t st) {
-    ResortArgs r;
-    r.sc = h->sc;
-    r.blk = h->blk;
-    r.in = state;
-    r.out = nullptr;
-    r.stride = h->stride;
-    r.cnt = h->rs_cnt;
-    r.cell_start = h->rs_start;
-    r.bsum = h->rs_bsum;
-    r.G = h->G;
-    r.key = h->rs_key;
-    r.rank = h->rs_rank;
-    r.sorted = h->rs_sorted;
-    r.dest = h->rs_vdest;
-    r.perm_in = nullptr;
-    r.perm_out = nullptr;
-    h->launches += 6;  // seven kernels; timed() counts one
-    timed(h, K_OTHER, st, [&] { launch_order(r, order, h->n_blocks, h->block, h->max_n, h->B, st); });
 }
 
 // Work slot that holds the final state of a forward rollout (the same
@@ -1075,11 +1007,10 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
     if (binned(h) && (rc = ensure_bin_slots(h, 1))) return rc;
     const long long nres = resort_count(h, nsteps, K);
     if (nres && (rc = ensure_resort(h, record ? nseg : 1))) return rc;
-    if ((rc = ensure_vorder(h, K))) return rc;
     const bool store = record && h->store_grids && !binned(h) && !fused(h);
     if (store && (rc = ensure_grid_slots(h, nsteps))) return rc;
     long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch,
-                         h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0) + (vorder_on(h) ? 512 * h->reorder : 0) +
+                         h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0) +
                              (store ? (1LL << 40) : 0) + (h->lsort ? (1LL << 41) : 0) + ((long long)h->pdl << 42) +
                              ((long long)h->lstage << 44),
                          h->block * 4096 + h->gblock};
@@ -1133,7 +1064,7 @@ namespace {
 // Enqueue the reverse pass of the recorded rollout.  dL/dforce is read from
 // h->dfbuf ([B][max_steps][3], entry fo = substep - t0); dL/dparams goes to
 // h->dpbuf.  Returns the adjoint slot holding dL/d(step-0 state).
-bool overlap_on(const DstirHandle* h) { return h->overlap && !binned(h) && !vorder_on(h) && !persist_on(h); }
+bool overlap_on(const DstirHandle* h) { return h->overlap && !binned(h) && !persist_on(h); }
 
 int enqueue_backward(DstirHandle* h, cudaStream_t st) {
     const int n = h->rec_n, K = h->rec_K, t0 = h->rec_t0;
@@ -1218,8 +1149,6 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.vo2 = nullptr;
             a.adj_prev = nullptr;
             a.box = box_slot(h, s0 + k);
-            // the kept-grid path recomputes states without building orders
-            a.order = h->rec_store ? nullptr : vorder_slot(h, k, true);
             a.lsort = h->lsort;
             a.pdl = h->pdl >= 2;
             a.lstage = h->lstage;
@@ -1355,7 +1284,6 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
             return rc;
     }
     if (binned(h) && (rc = ensure_bin_slots(h, K))) return rc;
-    if ((rc = ensure_vorder(h, K))) return rc;
     // dL/dforce [B][n][3] -> internal [B][max_steps][3]
     CUDA_TRY(h, cudaMemcpy2DAsync(h->dfbuf, (size_t)h->max_steps * 3 * sizeof(float), dL_dforce,
                                   (size_t)n * 3 * sizeof(float), (size_t)n * 3 * sizeof(float), (size_t)h->B,
@@ -1364,7 +1292,7 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
                          h->block * 4096 + h->gblock,
                          (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0) + (ovl ? 4 : 0) + (h->lsort ? 8 : 0) +
                              16 * h->pdl + 64 * h->lstage,
-                         vorder_on(h) ? h->reorder : 0};
+                         0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, &h->bwd_kernels,
                          [&](cudaStream_t s2) { enqueue_backward(h, s2); });
@@ -1396,24 +1324,20 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream) {
 int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     if (!h || !key) return DSTIR_EINVAL;
     if (!strcmp(key, "p2g")) {
-        if (value < 0 || value > 4) return fail(h, DSTIR_EINVAL, "p2g variant %lld not in 0..4", (long long)value);
+        // variant 2 (one thread per binned cell) was measured slower on every
+        // shape and retired; its number stays unused
+        if (value < 0 || value > 4 || value == 2)
+            return fail(h, DSTIR_EINVAL, "p2g variant %lld not in {0, 1, 3, 4}", (long long)value);
         h->p2g_variant = (int)value;
         h->recorded = false;
-        if (value == P2G_CELL && h->gblock > 256) {  // its cell kernels run in blocks of gblock <= 256
-            h->gblock = 256;
-            return build_tables(h);
-        }
         return DSTIR_OK;
     }
     if (!strcmp(key, "block") || !strcmp(key, "gblock")) {
         // grid blocks may be larger (fewer partial sums in the rod-force
-        // reduction); the cell-binned kernels run one thread per cell in
-        // blocks of gblock and are built for at most 256
+        // reduction)
         const bool grid_key = !strcmp(key, "gblock");
         if (value != 64 && value != 128 && value != 256 && !(grid_key && (value == 512 || value == 1024)))
             return fail(h, DSTIR_EINVAL, "%s must be 64, 128 or 256 (gblock also 512 or 1024)", key);
-        if (grid_key && value > 256 && h->p2g_variant == P2G_CELL)
-            return fail(h, DSTIR_EINVAL, "gblock above 256 does not work with p2g variant 2");
         if (!strcmp(key, "block"))
             h->block = (int)value;
         else
@@ -1471,13 +1395,6 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
     }
     if (!strcmp(key, "store_grids")) {
         h->store_grids = value ? 1 : 0;
-        h->recorded = false;
-        return DSTIR_OK;
-    }
-    if (!strcmp(key, "reorder")) {
-        if (value < 0 || value > 1000000) return fail(h, DSTIR_EINVAL, "reorder %lld out of range", (long long)value);
-        h->reorder = (int)value;
-        ++h->epoch;
         h->recorded = false;
         return DSTIR_OK;
     }
@@ -1543,7 +1460,6 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "resort")) *value = h->resort;
     else if (!strcmp(key, "tight")) *value = h->tight;
     else if (!strcmp(key, "box")) *value = h->use_box;
-    else if (!strcmp(key, "reorder")) *value = h->reorder;
     else if (!strcmp(key, "store_grids")) *value = h->store_grids;
     else if (!strcmp(key, "overlap")) *value = h->overlap;
     else if (!strcmp(key, "persist")) *value = h->persist;

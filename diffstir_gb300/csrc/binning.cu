@@ -1,18 +1,16 @@
-// Per-substep particle binning by cell, and the binned scatter kernels.
+// Per-substep particle binning by brick, and the brick-tiled scatter and
+// gather kernels (p2g variant 3).
 //
 // The reference scatters every particle to its 27 stencil nodes with one
 // global atomic per node and component (p2g, simulation_functions.py:155-163;
 // Taichi's g2p.grad does the transposed scatter).  Here the particles of each
-// substep are first counting-sorted by the cell of their stencil base
-// (bin_count -> 3-phase scan -> bin_scatter).  All particles of a cell share
-// the same 27 target nodes, so the binned kernels run one thread per cell: the
-// thread accumulates its particles' contributions in registers and issues one
-// vector atomic per node, i.e. 27 per occupied cell instead of 27 per
-// particle, and within a warp (32 neighbouring cells) no two lanes target the
-// same node in the same instruction.
+// substep are first counting-sorted by the 4x4x4-cell brick of their stencil
+// base (bin_count -> 3-phase scan -> bin_scatter).  One CTA per brick then
+// accumulates its particles' contributions in a 6x6x6-node tile in shared
+// memory and flushes each touched node with one vector atomic.
 //
-// Particles whose stencil leaves the grid go to an overflow bin (index G) that
-// the extra last block of each binned kernel handles without scattering.
+// Particles whose stencil leaves the grid go to an overflow bin that the
+// extra last blocks of each binned kernel handle without scattering.
 #include <cuda_runtime.h>
 
 #include "common.cuh"
@@ -205,7 +203,7 @@ void launch_scan(int* cnt, long long n, int* bsum, int* cell_start, cudaStream_t
 }
 
 // ---------------------------------------------------------------------------
-// binned P2G: one thread per cell
+// per-particle pieces of the brick kernels
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int particle_kind(const SceneDev& s, long long p) {
     long long q = p - s.p0;
@@ -240,91 +238,6 @@ __device__ __forceinline__ void p2g_particle(const FwdArgs& a, const SceneDev& s
     }
 }
 
-template <bool SVDJ>
-__global__ void __launch_bounds__(256) p2g_cell_kernel(FwdArgs a, const int* __restrict__ cell_start,
-                                                       const int* __restrict__ perm, int n_gblocks, long long G) {
-    __shared__ SceneDev s;
-    __shared__ GridBlock gb;
-    __shared__ float prm[4];
-    __shared__ int model;
-    const bool overflow = blockIdx.x >= (unsigned)n_gblocks;
-    if (threadIdx.x == 0) {
-        gb = a.gblk[overflow ? 0 : blockIdx.x];
-        s = a.sc[gb.scene];
-    }
-    __syncthreads();
-    if (overflow) {
-        // particles outside the grid: F[f+1] only, no scatter (status was raised when binning)
-        int beg = cell_start[G], end = cell_start[G + 1];
-        const unsigned first = blockIdx.x - (unsigned)(gridDim.x - OVERFLOW_CTAS);
-        for (int q = beg + first * blockDim.x + threadIdx.x; q < end; q += OVERFLOW_CTAS * blockDim.x) {
-            long long p = perm[q];
-            int sc_i = 0;
-            while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
-            SceneDev s2 = a.sc[sc_i];
-            float pr[4];
-#pragma unroll
-            for (int i = 0; i < 4; ++i) pr[i] = a.params[sc_i * 4 + i];
-            float x[3], m, mv[3], A[9];
-            p2g_particle<SVDJ>(a, s2, pr, a.models[sc_i], p, particle_kind(s2, p), x, m, mv, A);
-        }
-        return;
-    }
-    if (threadIdx.x < 4) prm[threadIdx.x] = a.params[gb.scene * 4 + threadIdx.x];
-    if (threadIdx.x == 0) model = a.models[gb.scene];
-    __syncthreads();
-    long long cell = gb.start + threadIdx.x;
-    if (cell >= gb.end) return;
-    int beg = cell_start[cell], end = cell_start[cell + 1];
-    if (beg == end) return;
-    long long local = cell - s.goff;
-    int n = s.n;
-    int bi = (int)(local / ((long long)n * n)), bj = (int)((local / n) % n), bk = (int)(local % n);
-    float acc[27][4];
-#pragma unroll
-    for (int o = 0; o < 27; ++o) acc[o][0] = acc[o][1] = acc[o][2] = acc[o][3] = 0.f;
-    for (int q = beg; q < end; ++q) {
-        long long p = perm[q];
-        float x[3], m, mv[3], A[9];
-        p2g_particle<SVDJ>(a, s, prm, model, p, particle_kind(s, p), x, m, mv, A);
-        float fx[3] = {x[0] * s.inv_dx - (float)bi, x[1] * s.inv_dx - (float)bj, x[2] * s.inv_dx - (float)bk};
-        float w[3][3];
-        bspline(fx, w);
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                float wij = w[i][0] * w[j][1];
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const int o = (i * 3 + j) * 3 + k;
-                    float W = wij * w[k][2];
-                    float dp0 = ((float)i - fx[0]) * s.dx, dp1 = ((float)j - fx[1]) * s.dx,
-                          dp2 = ((float)k - fx[2]) * s.dx;
-                    acc[o][0] += W * (mv[0] + (A[0] * dp0 + A[1] * dp1 + A[2] * dp2));
-                    acc[o][1] += W * (mv[1] + (A[3] * dp0 + A[4] * dp1 + A[5] * dp2));
-                    acc[o][2] += W * (mv[2] + (A[6] * dp0 + A[7] * dp1 + A[8] * dp2));
-                    acc[o][3] += W * m;
-                }
-            }
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            long long row = node_index(s, bi + i, bj + j, bk);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int o = (i * 3 + j) * 3 + k;
-                red_add4(a.pm + row + k, acc[o][0], acc[o][1], acc[o][2], acc[o][3]);
-            }
-        }
-}
-
-// ---------------------------------------------------------------------------
-// binned G2P adjoint (G2P^T): one thread per cell scatters into the grid
-// adjoint; the per-particle position adjoint is written as in g2p_adj_kernel
-// ---------------------------------------------------------------------------
 __device__ __forceinline__ void g2p_adj_particle_inputs(const AdjArgs& a, const SceneDev& s, const float* fb,
                                                         long long p, int kind, float vnb[3], float xb[3],
                                                         float Cb[9]) {
@@ -348,106 +261,6 @@ __device__ __forceinline__ void g2p_adj_particle_inputs(const AdjArgs& a, const 
 #pragma unroll
         for (int c = 0; c < 3; ++c) vnb[c] = xb[c] = 0.f;
     }
-}
-
-__global__ void __launch_bounds__(256) g2p_adj_cell_kernel(AdjArgs a, const int* __restrict__ cell_start,
-                                                           const int* __restrict__ perm, int n_gblocks,
-                                                           long long G) {
-    __shared__ SceneDev s;
-    __shared__ GridBlock gb;
-    __shared__ float fb[3];
-    const bool overflow = blockIdx.x >= (unsigned)n_gblocks;
-    if (overflow) {
-        // particles outside the grid: only x[f+1] = x[f] + dt v[f+1] carries an adjoint
-        int beg = cell_start[G], end = cell_start[G + 1];
-        const unsigned first = blockIdx.x - (unsigned)(gridDim.x - OVERFLOW_CTAS);
-        for (int q = beg + first * blockDim.x + threadIdx.x; q < end; q += OVERFLOW_CTAS * blockDim.x) {
-            long long p = perm[q];
-            int sc_i = 0;
-            while (sc_i + 1 < a.batch && a.sc[sc_i + 1].p0 <= p) ++sc_i;
-            if (particle_kind(a.sc[sc_i], p) == KIND_LIQUID) {
-                float ax[3];
-                load3(a.adj_next, a.stride, OX, p, ax);
-                store3(a.adj_cur, a.stride, OX, p, ax);
-            }
-        }
-        return;
-    }
-    if (threadIdx.x == 0) {
-        gb = a.gblk[blockIdx.x];
-        s = a.sc[gb.scene];
-        const float* d = a.dforce + gb.scene * a.dforce_stride + (long long)a.fo * 3;
-        for (int c = 0; c < 3; ++c) fb[c] = d[c];
-    }
-    __syncthreads();
-    long long cell = gb.start + threadIdx.x;
-    if (cell >= gb.end) return;
-    int beg = cell_start[cell], end = cell_start[cell + 1];
-    if (beg == end) return;
-    long long local = cell - s.goff;
-    int n = s.n;
-    int bi = (int)(local / ((long long)n * n)), bj = (int)((local / n) % n), bk = (int)(local % n);
-    const float c4 = 4.f * s.inv_dx;
-    float acc[27][3];
-#pragma unroll
-    for (int o = 0; o < 27; ++o) acc[o][0] = acc[o][1] = acc[o][2] = 0.f;
-    for (int q = beg; q < end; ++q) {
-        long long p = perm[q];
-        int kind = particle_kind(s, p);
-        float x[3], vnb[3], xb[3], Cb[9];
-        load3(a.cur, a.stride, OX, p, x);
-        g2p_adj_particle_inputs(a, s, fb, p, kind, vnb, xb, Cb);
-        float fx[3] = {x[0] * s.inv_dx - (float)bi, x[1] * s.inv_dx - (float)bj, x[2] * s.inv_dx - (float)bk};
-        float w[3][3], dw[3][3];
-        bspline_d(fx, w, dw);
-        float fxb[3] = {0.f, 0.f, 0.f};
-        const bool liquid = kind == KIND_LIQUID;
-#pragma unroll
-        for (int i = 0; i < 3; ++i)
-#pragma unroll
-            for (int j = 0; j < 3; ++j) {
-                long long row = node_index(s, bi + i, bj + j, bk);
-#pragma unroll
-                for (int k = 0; k < 3; ++k) {
-                    const int o = (i * 3 + j) * 3 + k;
-                    float W = w[i][0] * w[j][1] * w[k][2];
-                    float d0 = (float)i - fx[0], d1 = (float)j - fx[1], d2 = (float)k - fx[2];
-                    float Cd0 = Cb[0] * d0 + Cb[1] * d1 + Cb[2] * d2;
-                    float Cd1 = Cb[3] * d0 + Cb[4] * d1 + Cb[5] * d2;
-                    float Cd2 = Cb[6] * d0 + Cb[7] * d1 + Cb[8] * d2;
-                    acc[o][0] += W * (vnb[0] + c4 * Cd0);
-                    acc[o][1] += W * (vnb[1] + c4 * Cd1);
-                    acc[o][2] += W * (vnb[2] + c4 * Cd2);
-                    if (liquid) {
-                        float4 g = __ldg(a.vo + row + k);
-                        float Wb = vnb[0] * g.x + vnb[1] * g.y + vnb[2] * g.z +
-                                   c4 * (g.x * Cd0 + g.y * Cd1 + g.z * Cd2);
-                        fxb[0] -= c4 * W * (Cb[0] * g.x + Cb[3] * g.y + Cb[6] * g.z);
-                        fxb[1] -= c4 * W * (Cb[1] * g.x + Cb[4] * g.y + Cb[7] * g.z);
-                        fxb[2] -= c4 * W * (Cb[2] * g.x + Cb[5] * g.y + Cb[8] * g.z);
-                        fxb[0] += Wb * dw[i][0] * w[j][1] * w[k][2];
-                        fxb[1] += Wb * w[i][0] * dw[j][1] * w[k][2];
-                        fxb[2] += Wb * w[i][0] * w[j][1] * dw[k][2];
-                    }
-                }
-            }
-        if (liquid) {
-#pragma unroll
-            for (int c = 0; c < 3; ++c) xb[c] += s.inv_dx * fxb[c];
-            store3(a.adj_cur, a.stride, OX, p, xb);
-        }
-    }
-#pragma unroll
-    for (int i = 0; i < 3; ++i)
-#pragma unroll
-        for (int j = 0; j < 3; ++j) {
-            long long row = node_index(s, bi + i, bj + j, bk);
-#pragma unroll
-            for (int k = 0; k < 3; ++k) {
-                const int o = (i * 3 + j) * 3 + k;
-                red_add4(a.ga + row + k, acc[o][0], acc[o][1], acc[o][2], 0.f);
-            }
-        }
 }
 
 // ---------------------------------------------------------------------------
@@ -953,20 +766,6 @@ void launch_g2p_adj_brick(const AdjArgs& a, const BrickInfo* bricks, int n_brick
         g2p_adj_brick_kernel<SCATTER_GLOBAL><<<g, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
     else
         g2p_adj_brick_kernel<SCATTER_ATOM><<<g, 256, 0, st>>>(a, bricks, cell_start, perm, n_bricks, nbins);
-}
-
-void launch_p2g_cell(const FwdArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
-                     long long G, bool svdj, cudaStream_t st) {
-    if (n_gblocks <= 0) return;
-    if (svdj)
-        p2g_cell_kernel<true><<<n_gblocks + OVERFLOW_CTAS, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
-    else
-        p2g_cell_kernel<false><<<n_gblocks + OVERFLOW_CTAS, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
-}
-
-void launch_g2p_adj_cell(const AdjArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
-                         long long G, cudaStream_t st) {
-    if (n_gblocks > 0) g2p_adj_cell_kernel<<<n_gblocks + OVERFLOW_CTAS, gblock, 0, st>>>(a, cell_start, perm, n_gblocks, G);
 }
 
 }  // namespace dstir

@@ -39,14 +39,11 @@ struct FwdArgs {
     // update skips nodes outside `box`.  NULL: no box (every node is updated)
     int* box = nullptr;
     int* box_next = nullptr;
-    // processing order of the liquid particles (thread slot q works on particle
-    // order[q], a permutation inside each scene's liquid range) or NULL
-    const int* order = nullptr;
     // grid update: blocks [0, n_gblocks) update nodes, the next `batch` blocks
     // compute the rod reaction force of one scene each (set by launch_grid)
     int n_gblocks = 0;
     // warp-aggregated P2G: rebuild the interleaved order inside each block of
-    // liquid particles before the scatter (ignored with `order`)
+    // liquid particles before the scatter
     int lsort = 0;
     // launch with programmatic dependent launch (see pdl_enter)
     int pdl = 0;
@@ -84,7 +81,6 @@ struct AdjArgs {
     const float4* vo2 = nullptr;     // grid velocity of substep f-1
     float* adj_prev = nullptr;       // adjoint slot of state f-1 (receives its position-adjoint part)
     const int* box = nullptr;        // occupied node box of substep f (see FwdArgs::box) or NULL
-    const int* order = nullptr;      // processing order (see FwdArgs::order) or NULL
     int lsort = 0;                   // warp-aggregated G2P adjoint: see FwdArgs::lsort
     int pdl = 0;                     // see FwdArgs::pdl
     int lstage = 0;                  // G2P adjoint: see FwdArgs::lstage
@@ -104,13 +100,14 @@ struct BinArgs {
     int* bsum;               // scan scratch, bin_scan_blocks(G) entries
     long long G;             // number of bins (the overflow bin is G)
     unsigned* status;
-    int key_mode;            // 0: bin = grid node of the stencil base; 1: brick-major key
+    int key_mode;            // 1: brick-major key (0, the grid node of the stencil base, is unused)
 };
 
 // p2g variants: scalar atomics per particle, vector atomics per particle,
-// binned one-thread-per-cell accumulation, brick tiles in shared memory,
-// vector atomics after warp run aggregation of the k-consecutive stencil rows
-enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_CELL = 2, P2G_BRICK = 3, P2G_WARP = 4 };
+// brick tiles in shared memory, vector atomics after warp run aggregation of
+// the k-consecutive stencil rows
+// (number 2, one thread per binned cell, was retired: slower on every shape)
+enum { P2G_PLAIN = 0, P2G_VEC = 1, P2G_BRICK = 3, P2G_WARP = 4 };
 
 // tight: register-cap level of the particle kernels (0, 1 or 2; see kernels.cu)
 void launch_p2g(const FwdArgs& a, int n_blocks, int block, int variant, bool svdj, cudaStream_t st, int tight = 0);
@@ -131,10 +128,6 @@ void launch_p2g_adj_g2p_adj(const AdjArgs& a, int n_blocks, int block, int varia
 
 void launch_bin(const BinArgs& b, int n_blocks, int block, cudaStream_t st);
 int bin_scan_blocks(long long G);
-void launch_p2g_cell(const FwdArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
-                     long long G, bool svdj, cudaStream_t st);
-void launch_g2p_adj_cell(const AdjArgs& a, const int* cell_start, const int* perm, int n_gblocks, int gblock,
-                         long long G, cudaStream_t st);
 
 // scatter mode of the brick kernels: 0 shared tile + atomicAdd, 1 shared tile +
 // red.shared, 2 direct global vector atomics in the brick's lane order
@@ -180,11 +173,6 @@ struct ResortArgs {
     int* perm_out;           // [N] caller index of each new position
 };
 void launch_resort(const ResortArgs& r, int n_blocks, int block, int max_n, int n_scenes, cudaStream_t st);
-// The same interleaved order as a processing order only: r.dest receives the
-// new slot of each particle and order[slot] the particle; the state is not
-// moved (r.out, r.perm_in and r.perm_out are unused).
-void launch_order(const ResortArgs& r, int* order, int n_blocks, int block, int max_n, int n_scenes,
-                  cudaStream_t st);
 // out[c][p] = in[c][dest[p]]: the adjoint of the re-sort (adjoint in the new
 // order -> adjoint in the order before)
 void launch_unpermute(const float* in, float* out, const int* dest, long long stride, long long n,

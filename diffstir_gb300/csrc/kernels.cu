@@ -44,7 +44,6 @@ __device__ __forceinline__ void p2g_body(const FwdArgs& a, int vb) {
     long long p = bi.start + threadIdx.x;
     bool active = p < bi.end;
     if (!active) p = bi.end - 1;  // the lane computes a copy and writes nothing
-    if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
     // re-interleaved blocks may stage their state through shared memory
     // (lstage): thread t loads slot t (coalesced, in flight during the sort),
     // thread s then reads the slot it processes; F[f+1] goes back the same way
@@ -53,7 +52,7 @@ __device__ __forceinline__ void p2g_body(const FwdArgs& a, int vb) {
     int slot = threadIdx.x;
     if constexpr (WARP) {
         __shared__ LocalOrderSmem lo;
-        if (a.lsort && !a.order && bi.kind == KIND_LIQUID) {
+        if (a.lsort && bi.kind == KIND_LIQUID) {
             const int count = (int)(bi.end - bi.start);
             staged = (a.lstage & 1) && blockDim.x <= 256;
             if (staged && (int)threadIdx.x < count)
@@ -337,8 +336,7 @@ __device__ __forceinline__ void g2p_body(const FwdArgs& a, int vb) {
     bool active = p < bi.end;
     float dv[3] = {0.f, 0.f, 0.f};
     if (active) {
-        if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
-        float x[3];
+            float x[3];
         load3<NC>(a.cur, a.stride, OX, p, x);
         int base[3];
         float fx[3];
@@ -637,7 +635,6 @@ __device__ __forceinline__ void g2p_adj_body(const AdjArgs& a, int vb) {
     bool active = p < bi.end;
     if (!WARP && !active) return;
     if (!active) p = bi.end - 1;  // WARP: the lane computes a copy and scatters nothing
-    if (a.order && bi.kind == KIND_LIQUID) p = a.order[p];
     // re-interleaved blocks may stage their inputs through shared memory
     // (lstage, as in P2G): row c < 3 holds x of the state, row 3 + c
     // component c of the next state's adjoint; rows 0-2 later carry the
@@ -647,7 +644,7 @@ __device__ __forceinline__ void g2p_adj_body(const AdjArgs& a, int vb) {
     int slot = threadIdx.x;
     if constexpr (WARP) {
         __shared__ LocalOrderSmem lo;
-        if (a.lsort && !a.order && bi.kind == KIND_LIQUID) {
+        if (a.lsort && bi.kind == KIND_LIQUID) {
             const int count = (int)(bi.end - bi.start);
             staged = (a.lstage & 2) && blockDim.x <= 256;
             if (staged && (int)threadIdx.x < count) {
@@ -898,7 +895,6 @@ __device__ __forceinline__ void p2g_adj_body(const AdjArgs& a, int vb) {
     float pg[4] = {0.f, 0.f, 0.f, 0.f};
     if (p < bi.end) {
         const bool liquid = bi.kind == KIND_LIQUID;
-        if (a.order && liquid) p = a.order[p];
         float x[3];
         load3<NC>(a.cur, a.stride, OX, p, x);
         float m, mv[3], A[9];

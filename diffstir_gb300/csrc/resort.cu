@@ -16,9 +16,6 @@
 //                     order
 // The reverse pass undoes the permutation on the state adjoint
 // (resort_unpermute).  Rod and container particles keep their positions.
-// Between two re-sorts the same order is also rebuilt more often as a
-// processing order only (launch_order): the kernels' thread slot q then
-// works on particle order[q], which needs no data movement and no adjoint.
 // The reference has no counterpart: its particle order never changes.
 #include <cuda_runtime.h>
 
@@ -159,15 +156,6 @@ __global__ void __launch_bounds__(256) resort_apply_kernel(ResortArgs r) {
     r.perm_out[d] = r.perm_in[p];
 }
 
-__global__ void __launch_bounds__(256) resort_order_kernel(const BlockInfo* blk, const int* dest, int* order) {
-    __shared__ BlockInfo bi;
-    if (threadIdx.x == 0) bi = blk[blockIdx.x];
-    __syncthreads();
-    long long p = bi.start + threadIdx.x;
-    if (p >= bi.end) return;
-    order[dest[p]] = (int)p;
-}
-
 __global__ void __launch_bounds__(256) resort_unpermute_kernel(const float* in, float* out, const int* dest,
                                                                long long stride, long long n) {
     long long p = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -187,17 +175,6 @@ void launch_resort(const ResortArgs& r, int n_blocks, int block, int max_n, int 
     const int row_threads = ((max_n + 31) / 32) * 32;
     resort_rows_kernel<<<dim3((unsigned)((long long)max_n * max_n), (unsigned)n_scenes), row_threads, 0, st>>>(r);
     resort_apply_kernel<<<n_blocks, block, 0, st>>>(r);
-}
-
-void launch_order(const ResortArgs& r, int* order, int n_blocks, int block, int max_n, int n_scenes,
-                  cudaStream_t st) {
-    if (n_blocks <= 0) return;
-    resort_count_kernel<<<n_blocks, block, 0, st>>>(r);
-    launch_scan(r.cnt, r.G + 1, r.bsum, r.cell_start, st);
-    resort_cellorder_kernel<<<n_blocks, block, 0, st>>>(r);
-    const int row_threads = ((max_n + 31) / 32) * 32;
-    resort_rows_kernel<<<dim3((unsigned)((long long)max_n * max_n), (unsigned)n_scenes), row_threads, 0, st>>>(r);
-    resort_order_kernel<<<n_blocks, block, 0, st>>>(r.blk, r.dest, order);
 }
 
 void launch_unpermute(const float* in, float* out, const int* dest, long long stride, long long n,

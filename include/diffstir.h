@@ -145,13 +145,12 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams,
 int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
 
 /* Tuning knobs (defaults in brackets): "p2g" [4] (0 scalar atomics per
- * particle, 1 vector atomics per particle, 2 cell-binned one-thread-per-cell
- * accumulation, 3 brick-binned shared-memory tiles with one CTA per
- * 4x4x4-cell brick, 4 vector atomics after summing neighbouring lanes'
- * contributions to shared stencil nodes by warp shuffles; 2, 3 and 4 also
- * select the matching G2P-adjoint scatter; variant 2 also sets gblock to 256),
+ * particle, 1 vector atomics per particle, 3 brick-binned shared-memory tiles
+ * with one CTA per 4x4x4-cell brick, 4 vector atomics after summing
+ * neighbouring lanes' contributions to shared stencil nodes by warp shuffles;
+ * 3 and 4 also select the matching G2P-adjoint scatter; 2 is not a variant),
  * "block" [256] (threads per particle block: 64, 128 or 256), "gblock" [1024]
- * (threads per grid block: 64 to 1024, at most 256 with variant 2), "graph" [1] (1:
+ * (threads per grid block: 64 to 1024), "graph" [1] (1:
  * replay each rollout and each reverse pass as a cached CUDA graph), "fuse" /
  * "fuse_adj" [0] (1: G2P of substep f fused with P2G of f+1 / P2G adjoint of
  * f fused with the G2P adjoint of f-1), "resort" [1] (re-sort the particle
@@ -159,15 +158,12 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * still cross the ABI in the order given to dstir_set_state), "tight" [2]
  * (register-cap level of the particle kernels, 0..2), "box" [1] (P2G records
  * each scene's occupied node box and the grid update and its adjoint skip the
- * nodes outside it; per-particle variants only), "reorder" [0] (rebuild the
- * interleaved order every this many substeps as a processing order only: the
- * kernels read the state through an index; measured slower than the physical
- * re-sort alone at 64^3), "store_grids" [0] (a recorded rollout keeps
+ * nodes outside it; per-particle variants only), "store_grids" [0] (a recorded rollout keeps
  * the P2G and velocity grids of every substep, 32 bytes per grid node and
  * substep, and the reverse pass recomputes the states of each segment with
  * G2P alone instead of rerunning P2G and the grid update), "overlap" [1] (the
  * reverse pass recomputes segment s-1 on a second stream while it runs the
- * adjoint of segment s; per-particle variants without "reorder"),
+ * adjoint of segment s; per-particle variants),
  * "lsort" [1] (variant 4: each block of liquid particles rebuilds the
  * interleaved order over its own particles before the P2G scatter and the
  * G2P-adjoint scatter, so the lane-to-lane summation keeps working as

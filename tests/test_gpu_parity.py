@@ -65,23 +65,21 @@ def fixture_scene(name, model):
 
 
 VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse': 1, 'fuse_adj': 0},
-            {'p2g': 0, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 2}, {'p2g': 3},
+            {'p2g': 0, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 3},
             {'p2g': 3, 'brick_scatter': 0}, {'p2g': 3, 'brick_scatter': 2}, {'p2g': 3, 'brick_gather': 0},
             {'p2g': 3, 'graph': 1}, {'p2g': 4}, {'p2g': 4, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 4, 'resort': 0},
             {'p2g': 4, 'graph': 1}, {'p2g': 4, 'tight': 0}, {'p2g': 4, 'tight': 1},
-            {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'tight': 0}, {'p2g': 4, 'reorder': 3},
-            {'p2g': 1, 'reorder': 2, 'graph': 1}, {'p2g': 4, 'store_grids': 1},
-            {'p2g': 4, 'store_grids': 1, 'graph': 1, 'reorder': 3}, {'p2g': 4, 'lsort': 0},
+            {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'tight': 0}, {'p2g': 4, 'store_grids': 1},
+            {'p2g': 4, 'store_grids': 1, 'graph': 1}, {'p2g': 4, 'lsort': 0},
             {'p2g': 4, 'block': 128}, {'p2g': 4, 'block': 64, 'graph': 1}, {'p2g': 4, 'pdl': 0},
             {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 4, 'pdl': 2, 'graph': 1},
             {'p2g': 4, 'lstage': 0}, {'p2g': 4, 'graph': 1, 'block': 128, 'tight': 2}, {'p2g': 4, 'graph': 0},
             {'p2g': 1, 'persist': 1, 'graph': 0}, {'p2g': 1, 'persist': 1, 'graph': 1}]
-VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'cell-binned', 'brick-red', 'brick-atom',
+VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
-               'warp-tight0', 'warp-tight1', 'warp-fused-tight0', 'warp-reorder3', 'vec-reorder2-graph', 'warp-store',
-               'warp-store-graph-reorder3', 'warp-nolsort', 'warp-block128', 'warp-block64-graph', 'warp-nopdl',
-               'warp-fused-graph', 'warp-pdl2-graph', 'warp-nostage', 'warp-graph-block128-tight2', 'warp-eager',
-               'vec-persist', 'vec-persist-graph']
+               'warp-tight0', 'warp-tight1', 'warp-fused-tight0', 'warp-store', 'warp-store-graph', 'warp-nolsort',
+               'warp-block128', 'warp-block64-graph', 'warp-nopdl', 'warp-fused-graph', 'warp-pdl2-graph',
+               'warp-nostage', 'warp-graph-block128-tight2', 'warp-eager', 'vec-persist', 'vec-persist-graph']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
@@ -319,36 +317,6 @@ def test_box_skip_matches_full_grid(opts):
     assert rel(fs1, fs0) < 1e-4
 
 
-@pytest.mark.parametrize('opts', [{'p2g': 4}, {'p2g': 1}, {'p2g': 4, 'graph': 1}, {'p2g': 4, 'resort': 0}],
-                         ids=['warp', 'vec', 'warp-graph', 'warp-noresort'])
-def test_processing_order_matches_fixed_order(opts):
-    """Rebuilding the processing order every 3 substeps inside 12-substep
-    segments changes only the order of the float atomics; recorded rollout,
-    reverse pass and an unrecorded rollout, two scenes."""
-    T, K = 36, 12
-    scenes = [rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=10)),
-              rounded(S.small_synthetic_scene(n_grid=20, ppc=4, n_steps=T, seed=11))]
-    wts = torch.as_tensor(np.random.default_rng(6).normal(size=(2, T, 3)), dtype=torch.float32, device='cuda')
-    out = {}
-    for ro in (0, 3):
-        sim = Simulator(scenes, max_steps=T, options=dict(opts, reorder=ro))
-        f = sim.forward(T, ckpt_every=K, record=True).cpu().numpy()
-        dp, ds = sim.backward(wts, want_state0=True)
-        sim.reset()
-        sim.forward(T, ckpt_every=K)
-        st = {k: v.cpu().numpy() for k, v in sim.get_state().items()}
-        assert sim.status() == 0
-        out[ro] = (f, st, dp.cpu().numpy(), {k: v.cpu().numpy() for k, v in ds.items()})
-        sim.close()
-    f0, st0, dp0, ds0 = out[0]
-    f1, st1, dp1, ds1 = out[3]
-    assert rel(f1, f0) < 1e-5
-    for k in 'xvCF':
-        assert rel(st1[k], st0[k]) < 1e-4, k
-        assert rel(ds1[k], ds0[k]) < 1e-3, k
-    assert rel(dp1, dp0) < 1e-4
-
-
 @pytest.mark.parametrize('opts', [{'p2g': 4}, {'p2g': 1, 'graph': 1}, {'p2g': 4, 'resort': 0}, {'p2g': 0}],
                          ids=['warp', 'vec-graph', 'warp-noresort', 'plain'])
 def test_kept_grids_match_recompute(opts):
@@ -423,7 +391,7 @@ def test_p2g_variants_agree():
     sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=5))
     wts = np.random.default_rng(4).normal(size=(T, 3))
     f0, g0, _, _ = gpu_force_and_grad(sc, T, wts, options={'p2g': 0})
-    for opts in ({'p2g': 1}, {'p2g': 2}, {'p2g': 2, 'block': 128, 'gblock': 128}, {'p2g': 1, 'graph': 1},
+    for opts in ({'p2g': 1}, {'p2g': 4}, {'p2g': 4, 'block': 128, 'gblock': 128}, {'p2g': 1, 'graph': 1},
                  {'p2g': 3}, {'p2g': 3, 'block': 64, 'gblock': 128}):
         f1, g1, _, _ = gpu_force_and_grad(sc, T, wts, options=opts)
         assert rel(f1, f0) < 1e-5, opts
@@ -434,8 +402,8 @@ def test_graph_replay_matches_eager_and_is_reusable():
     T = 18
     sc = rounded(S.small_synthetic_scene(n_grid=16, ppc=2, n_steps=T, seed=7))
     wts = torch.as_tensor(np.random.default_rng(8).normal(size=(1, T, 3)), dtype=torch.float32, device='cuda')
-    eager = Simulator(sc, max_steps=T, options={'p2g': 2, 'graph': 0})
-    graph = Simulator(sc, max_steps=T, options={'p2g': 2, 'graph': 1})
+    eager = Simulator(sc, max_steps=T, options={'p2g': 3, 'graph': 0})
+    graph = Simulator(sc, max_steps=T, options={'p2g': 3, 'graph': 1})
     fe = eager.forward(T, ckpt_every=5, record=True)
     ge = eager.backward(wts)
     for rep in range(3):  # replays of the cached graphs with new parameters
@@ -469,7 +437,7 @@ def test_batched_equals_single():
                                  (1, 0.42, (2.0, 0.1, 0.6, 0.8), S.MODEL_CARREAU),
                                  (2, 0.22, (0.9, 0.4, 0.8, 0.0), S.MODEL_HB))]
     wts = np.random.default_rng(5).normal(size=(len(scenes), T, 3))
-    for opts in ({'p2g': 1}, {'p2g': 2, 'graph': 1}, {'p2g': 3}):
+    for opts in ({'p2g': 1}, {'p2g': 3, 'graph': 1}, {'p2g': 4}):
         sim = Simulator(scenes, max_steps=T, options=opts)
         force = sim.forward(T, ckpt_every=6, record=True).cpu().numpy()
         dp = sim.backward(torch.as_tensor(wts, dtype=torch.float32, device='cuda')).cpu().numpy()
