@@ -18,12 +18,13 @@ LIB = os.path.join(OUT_DIR, 'libdiffstir.so')
 SOURCES = ['kernels.cu', 'binning.cu', 'svd.cu', 'api.cu', 'static_substep.cu', 'resort.cu', 'calib.cu']
 HEADERS = ['common.cuh', 'svd.cuh', 'device_util.cuh', 'adjoint.cuh', 'internal.h']
 ARCH = ['-gencode', 'arch=compute_103a,code=sm_103a']
-# -prec-div=false / -prec-sqrt=false: single-precision division and square
-# root by the approximate (2-ulp) sequences.  The particle kernels are
-# instruction-bound in part (the P2G adjoint: 8% shorter), and the results stay
-# within the parity bars (1e-4 force, 1e-3 gradient against FP64).
+# -use_fast_math: single-precision division, square root, powf and logf by
+# the hardware's approximate sequences, denormals flushed.  The particle
+# kernels are instruction-bound in part (the P2G adjoint: 11% shorter), and the
+# results stay within the parity bars (1e-4 force, 1e-3 gradient against
+# FP64); the SVD backward's near-degenerate terms stay in FP64.
 NVCC_FLAGS = ['-O3', '-std=c++17', '-lineinfo', '-Xcompiler', '-fPIC', '-Xcompiler', '-O2',
-              '--expt-relaxed-constexpr', '-prec-div=false', '-prec-sqrt=false']
+              '--expt-relaxed-constexpr', '-use_fast_math']
 
 
 def nvcc_path():

@@ -150,7 +150,7 @@ __device__ __forceinline__ void p2g_body(const FwdArgs& a, int vb) {
 #pragma unroll
         for (int j = 0; j < 3; ++j) {
             float wij = w[i][0] * w[j][1];
-            long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+            const int row = node_index(s, base[0] + i, base[1] + j, base[2]);
             float r[3];
 #pragma unroll
             for (int q = 0; q < 3; ++q) r[q] = cc[q] + (float)i * Ad[q * 3 + 0] + (float)j * Ad[q * 3 + 1];
@@ -353,7 +353,7 @@ __device__ __forceinline__ void g2p_body(const FwdArgs& a, int vb) {
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
-                    long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    const long long row = node_index64(s, base[0] + i, base[1] + j, base[2]);
                     float wij = w[i][0] * w[j][1];
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
@@ -479,7 +479,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
-                    long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    const int row = node_index(s, base[0] + i, base[1] + j, base[2]);
                     float wij = w[i][0] * w[j][1];
 #pragma unroll
                     for (int k = 0; k < 3; ++k) {
@@ -578,7 +578,7 @@ __global__ void __launch_bounds__(256, MINB) g2p_p2g_kernel(FwdArgs a) {
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
                     float wij = w[i][0] * w[j][1];
-                    long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    const int row = node_index(s, base[0] + i, base[1] + j, base[2]);
                     float r[3];
 #pragma unroll
                     for (int q = 0; q < 3; ++q) r[q] = cc[q] + (float)i * Ad[q * 3 + 0] + (float)j * Ad[q * 3 + 1];
@@ -725,7 +725,7 @@ __device__ __forceinline__ void g2p_adj_body(const AdjArgs& a, int vb) {
         for (int i = 0; i < 3; ++i)
 #pragma unroll
             for (int j = 0; j < 3; ++j) {
-                long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                const int row = node_index(s, base[0] + i, base[1] + j, base[2]);
                 const float wij = w[i][0] * w[j][1], dxij = dw[i][0] * w[j][1], dyij = w[i][0] * dw[j][1];
                 float r[3];
 #pragma unroll
@@ -1021,7 +1021,7 @@ __global__ void __launch_bounds__(256, MINB) p2g_adj_g2p_adj_kernel(AdjArgs a) {
             for (int i = 0; i < 3; ++i)
 #pragma unroll
                 for (int j = 0; j < 3; ++j) {
-                    long long row = node_index(s, base[0] + i, base[1] + j, base[2]);
+                    const int row = node_index(s, base[0] + i, base[1] + j, base[2]);
                     const float wij = w[i][0] * w[j][1], dxij = dw[i][0] * w[j][1], dyij = w[i][0] * dw[j][1];
                     float r[3];
 #pragma unroll
