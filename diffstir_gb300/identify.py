@@ -325,10 +325,10 @@ def main(argv=None):
             print(json.dumps(out), flush=True)
         return out
     opts = None
-    if args.autotune:
+    ra, rb = sharding.shard_range(R, world, rank)
+    if args.autotune and rb > ra:
         from . import autotune
-        opts = autotune.autotune([copy.copy(sc) for _ in range(sharding.shard_range(R, world, rank)[1] -
-                                                                sharding.shard_range(R, world, rank)[0])])
+        opts = autotune.autotune([copy.copy(sc) for _ in range(rb - ra)])
     res = adam_identify(sc, target, restarts=R, iters=args.iters, lr=args.lr, ckpt_every=args.ckpt or cfg['ckpt'],
                         free=free, bounds=bounds, seed=args.seed + 1, options=opts)
     if res['sim'] is not None:
