@@ -76,11 +76,16 @@ __device__ __forceinline__ void group_sum(float (&v)[NV], float (*sh)[4], float*
 // Programmatic dependent launch (option "pdl").  The substep kernels are
 // launched with programmatic stream serialisation, so a kernel's blocks may
 // become resident while the kernel before it in the stream is still running.
-// Each of them therefore waits, before its first access to device memory,
-// until the grids it depends on have completed and their writes are visible
-// (griddepcontrol.wait; without the launch attribute it returns at once), and
-// then lets the next kernel of the stream be launched (launch_dependents:
-// that kernel's own wait still holds it until this grid has completed).
+// Each of them therefore waits, before its first access to memory that an
+// earlier kernel of the stream writes, until the grids it depends on have
+// completed and their writes are visible (griddepcontrol.wait; without the
+// launch attribute it returns at once), and then lets the next kernel of the
+// stream be launched (launch_dependents: that kernel's own wait still holds
+// it until this grid has completed).  Every kernel before the previous one
+// has completed by the time a kernel starts (the previous one passed its own
+// wait before letting it launch), so tables written before the rollout (block
+// tables, scenes, trajectories) may be read before the wait; the grid kernels
+// do so.
 __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");

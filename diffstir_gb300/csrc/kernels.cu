@@ -29,7 +29,10 @@ namespace dstir {
 // one-substep kernel passes blockIdx.x, a persistent segment kernel loops its
 // blocks over the virtual blocks of each phase (every body ends with no
 // pending barrier, and the caller separates two bodies by __syncthreads).
-// NC: load policy (ldp in device_util.cuh).
+// NC: load policy (ldp in device_util.cuh).  NC is true exactly in the
+// one-substep kernels: their bodies read the block descriptor, the scene and
+// the other tables written before the rollout, then wait on the previous
+// kernel (pdl_enter) before touching the state or the grids.
 template <int VARIANT, bool SVDJ, bool NC>
 __device__ __forceinline__ void p2g_body(const FwdArgs& a, int vb) {
     __shared__ SceneDev s;
@@ -39,6 +42,7 @@ __device__ __forceinline__ void p2g_body(const FwdArgs& a, int vb) {
         bi = a.blk[vb];
         s = a.sc[bi.scene];
     }
+    if (NC) pdl_enter();
     __syncthreads();
     constexpr bool WARP = VARIANT == P2G_WARP;
     long long p = bi.start + threadIdx.x;
@@ -183,7 +187,6 @@ __device__ __forceinline__ void p2g_body(const FwdArgs& a, int vb) {
 
 template <int VARIANT, bool SVDJ, int MINB>
 __global__ void __launch_bounds__(256, MINB) p2g_kernel(FwdArgs a) {
-    pdl_enter();
     p2g_body<VARIANT, SVDJ, true>(a, blockIdx.x);
 }
 
@@ -204,6 +207,7 @@ __device__ __forceinline__ bool in_rod_cylinder(const SceneDev& s, const float r
     return __fadd_rn(__fmul_rn(ex, ex), __fmul_rn(ez, ez)) < s.rod_r2 && __fmul_rn((float)j, s.dx) >= rc[1];
 }
 
+template <bool LOOP>
 __device__ __forceinline__ void rod_force_block(const FwdArgs& a, int scene, SceneDev& s, float (*sh)[4]) {
     load_scene_shared(s, a.sc + scene);
     __syncthreads();
@@ -215,6 +219,7 @@ __device__ __forceinline__ void rod_force_block(const FwdArgs& a, int scene, Sce
         rc[c] = t0[c];
         rodv[c] = (t0[3 + c] - t0[c]) / s.dt;
     }
+    if (!LOOP) pdl_enter();  // the P2G entries below are the previous kernel's output
     const int n = s.n;
     const float r = sqrtf(s.rod_r2);
     // bounding column with one node of slack each way; the cylinder test is
@@ -247,13 +252,19 @@ __device__ __forceinline__ void rod_force_block(const FwdArgs& a, int scene, Sce
 // for vb >= n_gblocks.  LOOP: the block's threads loop over the node block's
 // nodes (a persistent kernel, whose blocks may be smaller than the node
 // blocks); otherwise one thread per node.
+// A one-substep launch may start while the P2G it follows is still running
+// (programmatic dependent launch).  The block table, the scene and the
+// trajectory are written before the rollout and never by that kernel, so
+// they are read before pdl_enter; the occupied box and the node's P2G entry
+// are read right after it, both in flight before the block's barrier.
 template <bool LOOP>
 __device__ __forceinline__ void grid_body(const FwdArgs& a, int vb) {
     __shared__ SceneDev s;
     __shared__ float rc[3], rc1[3];
     __shared__ float sh[32][4];
+    __shared__ int bx[6];
     if (vb >= a.n_gblocks) {  // block-uniform: a rod-force block
-        rod_force_block(a, vb - a.n_gblocks, s, sh);
+        rod_force_block<LOOP>(a, vb - a.n_gblocks, s, sh);
         return;
     }
     // every thread reads the block descriptor (one broadcast load), so the
@@ -265,15 +276,20 @@ __device__ __forceinline__ void grid_body(const FwdArgs& a, int vb) {
         rc[threadIdx.x] = t0[threadIdx.x];
         rc1[threadIdx.x] = t0[3 + threadIdx.x];
     }
+    if (!LOOP) pdl_enter();
+    const bool use_box = a.box != nullptr;
+    if (use_box && threadIdx.x < 6) bx[threadIdx.x] = a.box[gb.scene * 6 + threadIdx.x];
+    const long long node0 = gb.start + threadIdx.x;
+    float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (!LOOP && node0 < gb.end) g0 = a.pm[node0];
     __syncthreads();
     const int n = s.n;
-    auto node_fn = [&](long long node) {
+    auto node_fn = [&](long long node, float4 g) {
         int i, j, k;
         node_ijk((int)(node - s.goff), n, i, j, k);
         // nodes outside the occupied box hold no mass and no stencil reads them:
         // their P2G entry is still zero and their velocity is never gathered
-        if (!a.box || box_inside(a.box + gb.scene * 6, i, j, k)) {
-            float4 g = a.pm[node];
+        if (!use_box || box_inside(bx, i, j, k)) {
             // nodes inside the rod belong to the rod-force block, which reads
             // and clears their P2G entries (their velocity is the rod's anyway)
             const bool in_rod = s.rod_mode == DSTIR_ROD_CYLINDER && in_rod_cylinder(s, rc, i, j, k);
@@ -305,15 +321,14 @@ __device__ __forceinline__ void grid_body(const FwdArgs& a, int vb) {
         }
     };
     if (LOOP) {
-        for (long long node = gb.start + threadIdx.x; node < gb.end; node += blockDim.x) node_fn(node);
-    } else if (gb.start + threadIdx.x < gb.end) {
-        node_fn(gb.start + threadIdx.x);
+        for (long long node = node0; node < gb.end; node += blockDim.x) node_fn(node, a.pm[node]);
+    } else if (node0 < gb.end) {
+        node_fn(node0, g0);
     }
 }
 
 __global__ void __launch_bounds__(1024) grid_kernel(FwdArgs a) {
-    pdl_enter();
-    grid_body<false>(a, blockIdx.x);
+    grid_body<false>(a, blockIdx.x);  // waits on the previous kernel itself
 }
 
 // WRITE_F: also write F of the next state, F_tmp = (I + dt C) F of the
@@ -331,6 +346,7 @@ __device__ __forceinline__ void g2p_body(const FwdArgs& a, int vb) {
         const float* t0 = a.traj + ((long long)bi.scene * a.traj_len + a.f) * 3;
         for (int c = 0; c < 3; ++c) tv[c] = (t0[3 + c] - t0[c]) / s.dt;
     }
+    if (NC) pdl_enter();
     __syncthreads();
     long long p = bi.start + threadIdx.x;
     bool active = p < bi.end;
@@ -430,7 +446,6 @@ __device__ __forceinline__ void g2p_body(const FwdArgs& a, int vb) {
 
 template <int MINB, bool WRITE_F>
 __global__ void __launch_bounds__(256, MINB) g2p_kernel(FwdArgs a) {
-    pdl_enter();
     g2p_body<WRITE_F, true>(a, blockIdx.x);
 }
 
@@ -629,6 +644,7 @@ __device__ __forceinline__ void g2p_adj_body(const AdjArgs& a, int vb) {
         const float* d = a.dforce + bi.scene * a.dforce_stride + (long long)a.fo * 3;
         for (int c = 0; c < 3; ++c) fb[c] = d[c];
     }
+    if (NC) pdl_enter();
     __syncthreads();
     constexpr bool WARP = VARIANT == P2G_WARP;
     long long p = bi.start + threadIdx.x;
@@ -783,36 +799,43 @@ __device__ __forceinline__ void g2p_adj_body(const AdjArgs& a, int vb) {
 
 template <int VARIANT, int MINB>
 __global__ void __launch_bounds__(256, MINB) g2p_adj_kernel(AdjArgs a) {
-    pdl_enter();
     g2p_adj_body<VARIANT, true>(a, blockIdx.x);
 }
 
-// Grid adjoint of the nodes of virtual block vb (LOOP: see grid_body).
+// Grid adjoint of the nodes of virtual block vb (LOOP, and the reads before
+// pdl_enter: see grid_body; dL/dforce is copied in before the reverse pass).
 template <bool LOOP>
 __device__ __forceinline__ void grid_adj_body(const AdjArgs& a, int vb) {
     __shared__ SceneDev s;
-    __shared__ float rc[3], rodv[3], fb[3];
+    __shared__ float rc[3], rc1[3], fb[3];
+    __shared__ int bx[6];
     const GridBlock gb = a.gblk[vb];
     load_scene_shared(s, a.sc + gb.scene);
-    __syncthreads();
     if (threadIdx.x < 3) {
         const int c = threadIdx.x;
         const float* t0 = a.traj + ((long long)gb.scene * a.traj_len + a.f) * 3;
         const float* d = a.dforce + gb.scene * a.dforce_stride + (long long)a.fo * 3;
         rc[c] = t0[c];
-        rodv[c] = (t0[3 + c] - t0[c]) / s.dt;
+        rc1[c] = t0[3 + c];
         fb[c] = d[c];
+    }
+    if (!LOOP) pdl_enter();
+    const bool use_box = a.box != nullptr;
+    if (use_box && threadIdx.x < 6) bx[threadIdx.x] = a.box[gb.scene * 6 + threadIdx.x];
+    const long long node0 = gb.start + threadIdx.x;
+    float4 g0 = make_float4(0.f, 0.f, 0.f, 0.f), b0 = g0;
+    if (!LOOP && node0 < gb.end) {
+        g0 = a.pm[node0];
+        b0 = a.ga[node0];
     }
     __syncthreads();
     const int n = s.n;
-    auto node_fn = [&](long long node) {
+    auto node_fn = [&](long long node, float4 g, float4 vb4) {
         int i, j, k;
         node_ijk((int)(node - s.goff), n, i, j, k);
         // outside the occupied box the velocity adjoint is zero (no stencil
         // scattered there) and no stencil gathers the P/M adjoint
-        if (a.box && !box_inside(a.box + gb.scene * 6, i, j, k)) return;
-        float4 g = a.pm[node];
-        float4 vb4 = a.ga[node];
+        if (use_box && !box_inside(bx, i, j, k)) return;
         a.ga[node] = make_float4(0.f, 0.f, 0.f, 0.f);
         float inv_m = 1.f / (g.w + 1e-10f);
         float u[3] = {inv_m * g.x, inv_m * g.y, inv_m * g.z};
@@ -848,8 +871,9 @@ __device__ __forceinline__ void grid_adj_body(const AdjArgs& a, int vb) {
         if (inside) {
 #pragma unroll
             for (int c = 0; c < 3; ++c) {
+                const float rodv = (rc1[c] - rc[c]) / s.dt;
                 ub[c] = -g.w * fb[c] / s.dt;
-                mb += fb[c] * (rodv[c] - u[c]) / s.dt;
+                mb += fb[c] * (rodv - u[c]) / s.dt;
             }
         } else {
             ub[0] = mask[0] * vb4.x;
@@ -865,15 +889,14 @@ __device__ __forceinline__ void grid_adj_body(const AdjArgs& a, int vb) {
         a.pmb[node] = make_float4(inv_m * ub[0], inv_m * ub[1], inv_m * ub[2], mb - inv_m * inv_m * Pu);
     };
     if (LOOP) {
-        for (long long node = gb.start + threadIdx.x; node < gb.end; node += blockDim.x) node_fn(node);
-    } else if (gb.start + threadIdx.x < gb.end) {
-        node_fn(gb.start + threadIdx.x);
+        for (long long node = node0; node < gb.end; node += blockDim.x) node_fn(node, a.pm[node], a.ga[node]);
+    } else if (node0 < gb.end) {
+        node_fn(node0, g0, b0);
     }
 }
 
 __global__ void __launch_bounds__(1024) grid_adj_kernel(AdjArgs a) {
-    pdl_enter();
-    grid_adj_body<false>(a, blockIdx.x);
+    grid_adj_body<false>(a, blockIdx.x);  // waits on the previous kernel itself
 }
 
 // P2G adjoint, one thread per particle (pieces in adjoint.cuh).
@@ -890,6 +913,7 @@ __device__ __forceinline__ void p2g_adj_body(const AdjArgs& a, int vb) {
         for (int i = 0; i < 4; ++i) prm[i] = a.params[bi.scene * 4 + i];
         model = a.models[bi.scene];
     }
+    if (NC) pdl_enter();
     __syncthreads();
     long long p = bi.start + threadIdx.x;
     float pg[4] = {0.f, 0.f, 0.f, 0.f};
@@ -919,7 +943,6 @@ __device__ __forceinline__ void p2g_adj_body(const AdjArgs& a, int vb) {
 
 template <bool SVDJ, int MINB>
 __global__ void __launch_bounds__(256, MINB) p2g_adj_kernel(AdjArgs a) {
-    pdl_enter();
     p2g_adj_body<SVDJ, true>(a, blockIdx.x);
 }
 
