@@ -63,7 +63,7 @@ def shape_key(scenes):
     rod = scenes[0].desc.rod_mode
     svd = int(any(s.desc.j_mode == 1 for s in scenes))
     name = torch.cuda.get_device_name() if torch.cuda.is_available() else 'cpu'
-    return 'v12|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
+    return 'v13|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
 
 
 def _load():

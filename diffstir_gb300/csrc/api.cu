@@ -171,6 +171,8 @@ struct DstirHandle {
     int lsort = 1;              // option "lsort": warp-aggregated scatters re-interleave each block's particles
     int pdl = 1;                // option "pdl": programmatic dependent launch, 1 forward rollouts, 2 everywhere
     int lstage = 3;             // option "lstage": re-interleaved blocks stage their state in shared memory (bit 0 P2G, bit 1 G2P adjoint)
+    int gprio = 1;              // option "gprio": grid kernels launched at the device's greatest priority
+    int prio_hi = 0;            // that priority (cudaDeviceGetStreamPriorityRange at create)
     bool rec_store = false;     // the recorded rollout kept its grids
     // reverse pass: the recompute of segment s-1 runs on rstream while the
     // adjoint of segment s runs on the caller's stream (double-buffered
@@ -363,6 +365,7 @@ FwdArgs fwd_args(DstirHandle* h, const float* cur, float* next, float4* pm, floa
     // level 1: forward rollouts only; level 2: also the reverse pass's recompute
     a.pdl = h->in_recompute ? h->pdl >= 2 : h->pdl >= 1;
     a.lstage = h->lstage;
+    a.gprio = h->gprio ? h->prio_hi : 0;
     return a;
 }
 
@@ -571,6 +574,10 @@ int dstir_create(const DstirSceneDesc* scenes, int32_t batch, int32_t max_steps,
     h->nbins_max = std::max(h->G, h->nbins_brick);
     h->n_bricks = (int)h->bricks_h.size();
     int rc = DSTIR_OK;
+    {
+        int least = 0, greatest = 0;
+        if (cudaDeviceGetStreamPriorityRange(&least, &greatest) == cudaSuccess) h->prio_hi = greatest;
+    }
     std::vector<int> models(batch);
     for (int s = 0; s < batch; ++s) models[s] = scenes[s].model;
     if ((rc = dalloc(h, &h->sc, batch, "scene table")) ||
@@ -966,7 +973,7 @@ int run_maybe_graph(DstirHandle* h, cudaStream_t st, cudaGraphExec_t* exec, long
         h->capturing = false;
         cudaError_t e = cudaStreamEndCapture(h->gstream, &g);
         if (e != cudaSuccess) return fail(h, DSTIR_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
-        e = cudaGraphInstantiate(exec, g, 0);
+        e = cudaGraphInstantiate(exec, g, h->gprio ? cudaGraphInstantiateFlagUseNodePriority : 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) {
             *exec = nullptr;
@@ -1012,7 +1019,7 @@ int dstir_forward(DstirHandle* h, int32_t t0, int32_t nsteps, int32_t ckpt_every
     long long want[8] = {t0, nsteps, K, record, h->cur, h->epoch,
                          h->p2g_variant * 16 + h->fuse + (nres ? 256 : 0) +
                              (store ? (1LL << 40) : 0) + (h->lsort ? (1LL << 41) : 0) + ((long long)h->pdl << 42) +
-                             ((long long)h->lstage << 44),
+                             ((long long)h->lstage << 44) + ((long long)h->gprio << 46),
                          h->block * 4096 + h->gblock};
     rc = run_maybe_graph(h, st, &h->fwd_exec, h->fwd_key, want, &h->fwd_kernels,
                          [&](cudaStream_t s2) { enqueue_forward(h, t0, nsteps, K, record != 0, store, s2); });
@@ -1152,6 +1159,7 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.lsort = h->lsort;
             a.pdl = h->pdl >= 2;
             a.lstage = h->lstage;
+            a.gprio = h->gprio ? h->prio_hi : 0;
             return a;
         };
         if (persist_on(h)) {
@@ -1291,7 +1299,7 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
     long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant * 16 + h->fuse * 2 + h->fuse_adj,
                          h->block * 4096 + h->gblock,
                          (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0) + (ovl ? 4 : 0) + (h->lsort ? 8 : 0) +
-                             16 * h->pdl + 64 * h->lstage,
+                             16 * h->pdl + 64 * h->lstage + 256 * h->gprio,
                          0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, &h->bwd_kernels,
@@ -1388,6 +1396,10 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         h->lstage = (int)value;
         return DSTIR_OK;
     }
+    if (!strcmp(key, "gprio")) {
+        h->gprio = value ? 1 : 0;
+        return DSTIR_OK;
+    }
     if (!strcmp(key, "pdl")) {
         if (value < 0 || value > 2) return fail(h, DSTIR_EINVAL, "pdl must be 0, 1 or 2");
         h->pdl = (int)value;
@@ -1469,6 +1481,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "lsort")) *value = h->lsort;
     else if (!strcmp(key, "pdl")) *value = h->pdl;
     else if (!strcmp(key, "lstage")) *value = h->lstage;
+    else if (!strcmp(key, "gprio")) *value = h->gprio;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

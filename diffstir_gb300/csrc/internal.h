@@ -47,6 +47,11 @@ struct FwdArgs {
     int lsort = 0;
     // launch with programmatic dependent launch (see pdl_enter)
     int pdl = 0;
+    // launch priority of the grid update (a cudaLaunchAttributePriority value;
+    // 0: the default).  In the overlapped reverse pass the grid kernels, short
+    // and each gating the next kernel of its stream, otherwise wait for SM
+    // slots behind the other stream's particle kernels
+    int gprio = 0;
     // with lsort: stage the block's state loads and F stores of P2G through
     // shared memory
     int lstage = 0;
@@ -83,6 +88,7 @@ struct AdjArgs {
     const int* box = nullptr;        // occupied node box of substep f (see FwdArgs::box) or NULL
     int lsort = 0;                   // warp-aggregated G2P adjoint: see FwdArgs::lsort
     int pdl = 0;                     // see FwdArgs::pdl
+    int gprio = 0;                   // launch priority of the grid adjoint (see FwdArgs::gprio)
     int lstage = 0;                  // G2P adjoint: see FwdArgs::lstage
 };
 

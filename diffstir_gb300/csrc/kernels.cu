@@ -1344,9 +1344,10 @@ cudaError_t launch_seg_adj(const SegAdjArgs& g, int grid, bool svdj, cudaStream_
 // level 2 also caps P2G at 48.
 // Launch with programmatic stream serialisation when `pdl` is set (the
 // kernels' pdl_enter keeps the ordering), else a plain launch.
+// prio: a cudaLaunchAttributePriority value for this launch (0: none).
 template <class Args>
-void klaunch(void (*k)(Args), unsigned grid, unsigned block, cudaStream_t st, const Args& a) {
-    if (!a.pdl) {
+void klaunch(void (*k)(Args), unsigned grid, unsigned block, cudaStream_t st, const Args& a, int prio = 0) {
+    if (!a.pdl && !prio) {
         k<<<grid, block, 0, st>>>(a);
         return;
     }
@@ -1355,11 +1356,20 @@ void klaunch(void (*k)(Args), unsigned grid, unsigned block, cudaStream_t st, co
     cfg.blockDim = dim3(block);
     cfg.dynamicSmemBytes = 0;
     cfg.stream = st;
-    cudaLaunchAttribute at[1];
-    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
-    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cudaLaunchAttribute at[2];
+    unsigned na = 0;
+    if (a.pdl) {
+        at[na].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+        at[na].val.programmaticStreamSerializationAllowed = 1;
+        ++na;
+    }
+    if (prio) {
+        at[na].id = cudaLaunchAttributePriority;
+        at[na].val.priority = prio;
+        ++na;
+    }
     cfg.attrs = at;
-    cfg.numAttrs = 1;
+    cfg.numAttrs = na;
     cudaLaunchKernelEx(&cfg, k, a);
 }
 
@@ -1379,7 +1389,7 @@ void launch_grid(const FwdArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
     if (n_gblocks <= 0) return;
     FwdArgs b = a;
     b.n_gblocks = n_gblocks;  // the last `batch` blocks compute the rod forces
-    klaunch(grid_kernel, n_gblocks + a.batch, gblock, st, b);
+    klaunch(grid_kernel, n_gblocks + a.batch, gblock, st, b, a.gprio);
 }
 void launch_g2p(const FwdArgs& a, int n_blocks, int block, cudaStream_t st, int tight, bool write_f) {
     if (n_blocks <= 0) return;
@@ -1415,7 +1425,7 @@ void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cuda
     klaunch(k, n_blocks, block, st, a);
 }
 void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st) {
-    if (n_gblocks > 0) klaunch(grid_adj_kernel, n_gblocks, gblock, st, a);
+    if (n_gblocks > 0) klaunch(grid_adj_kernel, n_gblocks, gblock, st, a, a.gprio);
 }
 void launch_p2g_adj(const AdjArgs& a, int n_blocks, int block, bool svdj, cudaStream_t st, int tight) {
     if (n_blocks <= 0) return;

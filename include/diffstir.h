@@ -170,7 +170,11 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * particles drift between re-sorts), "lstage" [3] (with "lsort": the
  * block's inputs are loaded coalesced into shared memory while the block
  * sorts, and its outputs go back the same way; bit 0 P2G, bit 1 the G2P
- * adjoint), "pdl" [1]
+ * adjoint), "gprio" [1] (the grid update and its adjoint are launched
+ * at the device's greatest priority, and graphs are instantiated with node
+ * priorities, so that in the overlapped reverse pass these short kernels,
+ * which each gate the next kernel of their stream, get SM slots ahead of the
+ * other stream's particle kernels; 0: default priority), "pdl" [1]
  * (programmatic dependent
  * launch of the substep kernels: a kernel's blocks may start while the
  * previous kernel of the stream drains and wait in hardware for its

@@ -75,13 +75,13 @@ VARIANTS = [{'p2g': 1, 'fuse': 1, 'fuse_adj': 1}, {'p2g': 1}, {'p2g': 1, 'fuse':
             {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'graph': 1}, {'p2g': 4, 'pdl': 2, 'graph': 1},
             {'p2g': 4, 'lstage': 0}, {'p2g': 4, 'graph': 1, 'block': 128, 'tight': 2}, {'p2g': 4, 'graph': 0},
             {'p2g': 1, 'persist': 1, 'graph': 0}, {'p2g': 1, 'persist': 1, 'graph': 1},
-            {'p2g': 1, 'persist': 1, 'store_grids': 1}]
+            {'p2g': 1, 'persist': 1, 'store_grids': 1}, {'p2g': 4, 'gprio': 0, 'graph': 1}]
 VARIANT_IDS = ['vec-fused', 'vec-unfused', 'vec-fwdfused', 'plain-fused-graph', 'brick-red', 'brick-atom',
                'brick-global', 'brick-nogather', 'brick-graph', 'warp', 'warp-fused', 'warp-nosort', 'warp-graph',
                'warp-tight0', 'warp-tight1', 'warp-fused-tight0', 'warp-store', 'warp-store-graph', 'warp-nolsort',
                'warp-block128', 'warp-block64-graph', 'warp-nopdl', 'warp-fused-graph', 'warp-pdl2-graph',
                'warp-nostage', 'warp-graph-block128-tight2', 'warp-eager', 'vec-persist', 'vec-persist-graph',
-               'vec-persist-store']
+               'vec-persist-store', 'warp-noprio-graph']
 
 
 @pytest.mark.parametrize('opts', VARIANTS, ids=VARIANT_IDS)
