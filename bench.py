@@ -81,7 +81,7 @@ def parse():
     ap.add_argument('--fuse', type=int, default=None, help='1: G2P(f) fused with P2G(f+1)')
     ap.add_argument('--fuse-adj', type=int, default=None, help='1: P2G adjoint of f fused with G2P adjoint of f-1')
     ap.add_argument('--resort', type=int, default=None, help='1: re-sort the particle order at every checkpoint')
-    ap.add_argument('--tight', type=int, default=None, help='register-cap level of the particle kernels: 0, 1 or 2')
+    ap.add_argument('--tight', type=int, default=None, help='register-cap level of the particle kernels: 0..3')
     ap.add_argument('--box', type=int, default=None, help='1: grid kernels skip nodes outside the occupied box')
     ap.add_argument('--store-grids', type=int, default=None, help='1: keep every substep\'s grids, recompute states only')
     ap.add_argument('--overlap', type=int, default=None, help='1: segment recompute on a second stream')
@@ -359,7 +359,7 @@ def batched_leg(args, rank, world, dev, stream):
     scenes = [S.synthetic_scene(args.batched_config, seed=rank * B + b, n_steps=T) for b in range(B)]
     # the tuner's candidates that win for batches of 64^3 scenes
     opts = autotune.autotune(scenes, candidates=[c for c in autotune.CANDIDATES
-                                                 if c.get('p2g') == 4 and c.get('tight') == 2])
+                                                 if c.get('p2g') == 4 and c.get('tight') in (2, 3)])
     sim = Simulator(scenes, max_steps=T, options=opts)
     rng = np.random.default_rng(2000 + rank)
     true_p = torch.tensor(np.stack([S.draw_config_params(args.batched_config, rng) for _ in range(B)]),

@@ -25,6 +25,8 @@ CANDIDATES = [
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 256, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 2},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 256, 'graph': 1, 'tight': 2},
+    {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 3},
+    {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 256, 'graph': 1, 'tight': 3},
     {'p2g': 4, 'fuse': 1, 'fuse_adj': 1, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 1, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 1},
     {'p2g': 4, 'fuse': 0, 'fuse_adj': 0, 'block': 256, 'gblock': 1024, 'graph': 1, 'tight': 0},
@@ -63,7 +65,7 @@ def shape_key(scenes):
     rod = scenes[0].desc.rod_mode
     svd = int(any(s.desc.j_mode == 1 for s in scenes))
     name = torch.cuda.get_device_name() if torch.cuda.is_available() else 'cpu'
-    return 'v13|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
+    return 'v14|%s|n%d|N2^%.1f|B%d|rod%d|svd%d' % (name, n, bucket / 2, len(scenes), rod, svd)
 
 
 def _load():

@@ -165,7 +165,7 @@ struct DstirHandle {
     // periodic re-sort of the particle order (per-particle variants): every K
     // substeps of a rollout, at the checkpoint boundaries of a recorded one
     int resort = 1;             // option "resort": 0 never
-    int tight = 2;              // option "tight": register-cap level of the particle kernels (0, 1, 2)
+    int tight = 3;              // option "tight": register-cap level of the particle kernels (0..3)
     int use_box = 1;            // option "box": the grid kernels skip nodes outside the occupied box
     int store_grids = 0;        // option "store_grids": a recorded rollout keeps every substep's grids
     int lsort = 1;              // option "lsort": warp-aggregated scatters re-interleave each block's particles
@@ -1417,7 +1417,7 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         return DSTIR_OK;
     }
     if (!strcmp(key, "tight")) {
-        if (value < 0 || value > 2) return fail(h, DSTIR_EINVAL, "tight %lld not in 0..2", (long long)value);
+        if (value < 0 || value > 3) return fail(h, DSTIR_EINVAL, "tight %lld not in 0..3", (long long)value);
         h->tight = (int)value;
         ++h->epoch;
         return DSTIR_OK;

@@ -1341,7 +1341,8 @@ cudaError_t launch_seg_adj(const SegAdjArgs& g, int grid, bool svdj, cudaStream_
 // for P2G, 80 for G2P and the fused forward, about 110-130 for the
 // adjoints); level 1 caps G2P and the fused forward at 64 and the adjoints at
 // 80 registers (a few spilled bytes, half again as many resident warps);
-// level 2 also caps P2G at 48.
+// level 2 also caps P2G at 48; level 3 also caps the G2P adjoint at 64 (36
+// spilled bytes; the P2G adjoint spills 340 bytes at 64 and stays at 80).
 // Launch with programmatic stream serialisation when `pdl` is set (the
 // kernels' pdl_enter keeps the ordering), else a plain launch.
 // prio: a cudaLaunchAttributePriority value for this launch (0: none).
@@ -1419,9 +1420,9 @@ void launch_g2p_adj(const AdjArgs& a, int n_blocks, int block, int variant, cuda
     if (variant == P2G_PLAIN)
         k = g2p_adj_kernel<P2G_PLAIN, 2>;
     else if (variant == P2G_WARP)
-        k = t1 ? g2p_adj_kernel<P2G_WARP, 3> : g2p_adj_kernel<P2G_WARP, 2>;
+        k = tight >= 3 ? g2p_adj_kernel<P2G_WARP, 4> : t1 ? g2p_adj_kernel<P2G_WARP, 3> : g2p_adj_kernel<P2G_WARP, 2>;
     else
-        k = t1 ? g2p_adj_kernel<P2G_VEC, 3> : g2p_adj_kernel<P2G_VEC, 2>;
+        k = tight >= 3 ? g2p_adj_kernel<P2G_VEC, 4> : t1 ? g2p_adj_kernel<P2G_VEC, 3> : g2p_adj_kernel<P2G_VEC, 2>;
     klaunch(k, n_blocks, block, st, a);
 }
 void launch_grid_adj(const AdjArgs& a, int n_gblocks, int gblock, cudaStream_t st) {

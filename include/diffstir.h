@@ -155,8 +155,8 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * "fuse_adj" [0] (1: G2P of substep f fused with P2G of f+1 / P2G adjoint of
  * f fused with the G2P adjoint of f-1), "resort" [1] (re-sort the particle
  * order every ckpt_every substeps of a rollout; states and state adjoints
- * still cross the ABI in the order given to dstir_set_state), "tight" [2]
- * (register-cap level of the particle kernels, 0..2), "box" [1] (P2G records
+ * still cross the ABI in the order given to dstir_set_state), "tight" [3]
+ * (register-cap level of the particle kernels, 0..3), "box" [1] (P2G records
  * each scene's occupied node box and the grid update and its adjoint skip the
  * nodes outside it; per-particle variants only), "store_grids" [0] (a recorded rollout keeps
  * the P2G and velocity grids of every substep, 32 bytes per grid node and
