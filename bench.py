@@ -89,6 +89,7 @@ def parse():
     ap.add_argument('--pdl', type=int, default=None, help='1: programmatic dependent launch of the substep kernels')
     ap.add_argument('--lstage', type=int, default=None, help='re-interleaved blocks stage their state in shared memory (bits: P2G, G2P adjoint)')
     ap.add_argument('--gprio', type=int, default=None, help='grid kernels at the greatest launch priority')
+    ap.add_argument('--prefetch', type=int, default=None, help='adjoint blocks hint L2 for the block this many later')
     ap.add_argument('--persist', type=int, default=None, help='1: persistent cooperative launches per chunk / segment')
     ap.add_argument('--cpu-sample', type=int, default=24, help='substeps in the CPU baseline sample')
     ap.add_argument('--ref-sample', type=int, default=12, help='substeps per reference-arm step')
@@ -461,7 +462,7 @@ def run_ours(args):
     sc = scenes[0]
     opts = {}
     keys = ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather', 'fuse', 'fuse_adj', 'resort', 'tight',
-            'box', 'store_grids', 'overlap', 'lsort', 'pdl', 'lstage', 'gprio', 'persist')
+            'box', 'store_grids', 'overlap', 'lsort', 'pdl', 'lstage', 'gprio', 'prefetch', 'persist')
     explicit = any(getattr(args, k) is not None for k in keys)
     if args.autotune and not explicit:
         from diffstir_gb300 import autotune
@@ -730,7 +731,7 @@ def run_ours(args):
     status_all = int(st) | int(sim.status())
     opts_used = {k: sim.get_option(k) for k in ('p2g', 'graph', 'block', 'gblock', 'brick_scatter', 'brick_gather',
                                                 'fuse', 'fuse_adj', 'resort', 'tight', 'box',
-                                                'store_grids', 'overlap', 'lsort', 'pdl', 'lstage', 'gprio', 'persist')}
+                                                'store_grids', 'overlap', 'lsort', 'pdl', 'lstage', 'gprio', 'prefetch', 'persist')}
     scatter_variant, scatter_fused = sim.get_option('p2g'), sim.get_option('fuse')
     sim.close()
     del sim

@@ -172,6 +172,7 @@ struct DstirHandle {
     int pdl = 1;                // option "pdl": programmatic dependent launch, 1 forward rollouts, 2 everywhere
     int lstage = 3;             // option "lstage": re-interleaved blocks stage their state in shared memory (bit 0 P2G, bit 1 G2P adjoint)
     int gprio = 1;              // option "gprio": grid kernels launched at the device's greatest priority
+    int pf_dist = 100;          // option "prefetch": adjoint blocks hint L2 for the block this many later
     int prio_hi = 0;            // that priority (cudaDeviceGetStreamPriorityRange at create)
     bool rec_store = false;     // the recorded rollout kept its grids
     // reverse pass: the recompute of segment s-1 runs on rstream while the
@@ -1160,6 +1161,8 @@ int enqueue_backward(DstirHandle* h, cudaStream_t st) {
             a.pdl = h->pdl >= 2;
             a.lstage = h->lstage;
             a.gprio = h->gprio ? h->prio_hi : 0;
+            a.pf_dist = h->pf_dist;
+            a.n_blocks = h->n_blocks;
             return a;
         };
         if (persist_on(h)) {
@@ -1299,7 +1302,7 @@ int dstir_backward(DstirHandle* h, const float* dL_dforce, float* dL_dparams, fl
     long long want[8] = {h->rec_t0, n, K, h->epoch, h->p2g_variant * 16 + h->fuse * 2 + h->fuse_adj,
                          h->block * 4096 + h->gblock,
                          (h->rec_resort ? 1 : 0) + (h->rec_store ? 2 : 0) + (ovl ? 4 : 0) + (h->lsort ? 8 : 0) +
-                             16 * h->pdl + 64 * h->lstage + 256 * h->gprio,
+                             16 * h->pdl + 64 * h->lstage + 256 * h->gprio + 512LL * h->pf_dist,
                          0};
     int final_nx = n % 2;
     rc = run_maybe_graph(h, st, &h->bwd_exec, h->bwd_key, want, &h->bwd_kernels,
@@ -1396,6 +1399,11 @@ int dstir_set_option(DstirHandle* h, const char* key, int64_t value) {
         h->lstage = (int)value;
         return DSTIR_OK;
     }
+    if (!strcmp(key, "prefetch")) {
+        if (value < 0 || value > 100000) return fail(h, DSTIR_EINVAL, "prefetch must be 0..100000");
+        h->pf_dist = (int)value;
+        return DSTIR_OK;
+    }
     if (!strcmp(key, "gprio")) {
         h->gprio = value ? 1 : 0;
         return DSTIR_OK;
@@ -1482,6 +1490,7 @@ int dstir_get_option(const DstirHandle* h, const char* key, int64_t* value) {
     else if (!strcmp(key, "pdl")) *value = h->pdl;
     else if (!strcmp(key, "lstage")) *value = h->lstage;
     else if (!strcmp(key, "gprio")) *value = h->gprio;
+    else if (!strcmp(key, "prefetch")) *value = h->pf_dist;
     else if (!strcmp(key, "n_blocks")) *value = h->n_blocks;
     else if (!strcmp(key, "n_gblocks")) *value = h->n_gblocks;
     else if (!strcmp(key, "stride")) *value = h->stride;

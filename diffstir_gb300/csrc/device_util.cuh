@@ -351,6 +351,18 @@ __device__ __forceinline__ void box_update(int* box, const int base[3], bool val
     }
 }
 
+// L2 prefetch hint for components [c0, c0 + ncomp) of the particles
+// [start, end) (at most 288 of them) of a [comp][stride] array: thread t
+// touches line t % 9 of component t / 9, so 9 * ncomp <= blockDim.x threads
+// cover it.  Every address lies inside [start, end).
+__device__ __forceinline__ void prefetch_state_l2(const float* st, long long stride, long long start,
+                                                  long long end, int c0, int ncomp) {
+    const int t = threadIdx.x, comp = t / 9, line = t - comp * 9;
+    if (comp >= ncomp || end <= start) return;
+    const long long p = min(start + 32LL * line, end - 1);
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(st + (long long)(c0 + comp) * stride + p));
+}
+
 __device__ __forceinline__ bool box_inside(const int* box, int i, int j, int k) {
     return i >= -box[0] && j >= -box[1] && k >= -box[2] && i <= box[3] && j <= box[4] && k <= box[5];
 }

@@ -89,6 +89,10 @@ struct AdjArgs {
     int lsort = 0;                   // warp-aggregated G2P adjoint: see FwdArgs::lsort
     int pdl = 0;                     // see FwdArgs::pdl
     int gprio = 0;                   // launch priority of the grid adjoint (see FwdArgs::gprio)
+    // the adjoint kernels' blocks hint L2 to fetch the state that the block
+    // pf_dist blocks later reads (0: no hints); n_blocks bounds that index
+    int pf_dist = 0;
+    int n_blocks = 0;
     int lstage = 0;                  // G2P adjoint: see FwdArgs::lstage
 };
 

@@ -645,6 +645,10 @@ __device__ __forceinline__ void g2p_adj_body(const AdjArgs& a, int vb) {
         for (int c = 0; c < 3; ++c) fb[c] = d[c];
     }
     if (NC) pdl_enter();
+    if (a.pf_dist && vb + a.pf_dist < a.n_blocks) {
+        const BlockInfo nb = a.blk[vb + a.pf_dist];
+        prefetch_state_l2(a.cur, a.stride, nb.start, nb.end, OX, 3);
+    }
     __syncthreads();
     constexpr bool WARP = VARIANT == P2G_WARP;
     long long p = bi.start + threadIdx.x;
@@ -914,6 +918,10 @@ __device__ __forceinline__ void p2g_adj_body(const AdjArgs& a, int vb) {
         model = a.models[bi.scene];
     }
     if (NC) pdl_enter();
+    if (a.pf_dist && vb + a.pf_dist < a.n_blocks) {
+        const BlockInfo nb = a.blk[vb + a.pf_dist];
+        prefetch_state_l2(a.cur, a.stride, nb.start, nb.end, 0, NS);
+    }
     __syncthreads();
     long long p = bi.start + threadIdx.x;
     float pg[4] = {0.f, 0.f, 0.f, 0.f};

@@ -170,7 +170,10 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * particles drift between re-sorts), "lstage" [3] (with "lsort": the
  * block's inputs are loaded coalesced into shared memory while the block
  * sorts, and its outputs go back the same way; bit 0 P2G, bit 1 the G2P
- * adjoint), "gprio" [1] (the grid update and its adjoint are launched
+ * adjoint), "prefetch" [100] (each block of the P2G adjoint and of the G2P
+ * adjoint hints L2, with prefetch.global.L2, to fetch the state that the
+ * block this many block indices later reads: the whole state for the P2G
+ * adjoint, the positions for the G2P adjoint; 0: no hints), "gprio" [1] (the grid update and its adjoint are launched
  * at the device's greatest priority, and graphs are instantiated with node
  * priorities, so that in the overlapped reverse pass these short kernels,
  * which each gate the next kernel of their stream, get SM slots ahead of the
