@@ -84,8 +84,8 @@ __device__ __forceinline__ void group_sum(float (&v)[NV], float (*sh)[4], float*
 // it until this grid has completed).  Every kernel before the previous one
 // has completed by the time a kernel starts (the previous one passed its own
 // wait before letting it launch), so tables written before the rollout (block
-// tables, scenes, trajectories) may be read before the wait; the grid kernels
-// do so.
+// tables, scenes, trajectories) may be read before the wait; the one-substep
+// kernels do so.
 __device__ __forceinline__ void pdl_enter() {
     asm volatile("griddepcontrol.wait;" ::: "memory");
     asm volatile("griddepcontrol.launch_dependents;" ::: "memory");
