@@ -125,3 +125,31 @@ def test_bench_option_flags_are_documented_options():
     m = re.search(r"keys = \(([^)]*)\)", src)
     names = set(re.findall(r"'([a-z_0-9]+)'", m.group(1)))
     assert names and names <= _documented_options(), names - _documented_options()
+
+
+def test_prefetch_hint_addresses_stay_in_the_block():
+    """Host restatement of prefetch_state_l2 (device_util.cuh): for blocks of
+    up to 256 particles at any start offset, every address that threads
+    0..255 touch lies inside the block's particle range, and the 128-byte
+    lines they touch are exactly the lines that hold the block's particles,
+    for every requested component."""
+    rng = np.random.default_rng(3)
+    for _ in range(200):
+        start = int(rng.integers(0, 10**6))
+        count = int(rng.integers(1, 257))
+        end = start + count
+        ncomp = int(rng.integers(1, 25))
+        stride = 10**6 + 512                          # a multiple of 32, as the handle's stride
+        touched = {}
+        for t in range(256):
+            comp, line = divmod(t, 9)
+            if comp >= ncomp:
+                continue
+            p = min(start + 32 * line, end - 1)
+            assert start <= p < end
+            touched.setdefault(comp, []).append(comp * stride + p)
+        assert sorted(touched) == list(range(ncomp))
+        for comp, addrs in touched.items():
+            base = comp * stride                         # a 128-byte-aligned base: stride % 32 == 0
+            lines = {a // 32 for a in addrs}             # float index -> 128-byte line
+            assert lines == {(base + q) // 32 for q in range(start, end)}
