@@ -648,6 +648,7 @@ __device__ __forceinline__ void g2p_adj_body(const AdjArgs& a, int vb) {
     if (a.pf_dist && vb + a.pf_dist < a.n_blocks) {
         const BlockInfo nb = a.blk[vb + a.pf_dist];
         prefetch_state_l2(a.cur, a.stride, nb.start, nb.end, OX, 3);
+        prefetch_state_l2(a.adj_next, a.stride, nb.start, nb.end, 0, 15);
     }
     __syncthreads();
     constexpr bool WARP = VARIANT == P2G_WARP;
@@ -921,6 +922,7 @@ __device__ __forceinline__ void p2g_adj_body(const AdjArgs& a, int vb) {
     if (a.pf_dist && vb + a.pf_dist < a.n_blocks) {
         const BlockInfo nb = a.blk[vb + a.pf_dist];
         prefetch_state_l2(a.cur, a.stride, nb.start, nb.end, 0, NS);
+        prefetch_state_l2(a.adj_next, a.stride, nb.start, nb.end, OF, 9);
     }
     __syncthreads();
     long long p = bi.start + threadIdx.x;

@@ -172,8 +172,10 @@ int dstir_status(DstirHandle* h, uint32_t* flags, void* stream);
  * sorts, and its outputs go back the same way; bit 0 P2G, bit 1 the G2P
  * adjoint), "prefetch" [100] (each block of the P2G adjoint and of the G2P
  * adjoint hints L2, with prefetch.global.L2, to fetch the state that the
- * block this many block indices later reads: the whole state for the P2G
- * adjoint, the positions for the G2P adjoint; 0: no hints), "gprio" [1] (the grid update and its adjoint are launched
+ * block this many block indices later reads: the whole state and the F part
+ * of the next state's adjoint for the P2G adjoint, the positions and the x,
+ * v, C parts of the next state's adjoint for the G2P adjoint; 0: no hints),
+ * "gprio" [1] (the grid update and its adjoint are launched
  * at the device's greatest priority, and graphs are instantiated with node
  * priorities, so that in the overlapped reverse pass these short kernels,
  * which each gate the next kernel of their stream, get SM slots ahead of the
