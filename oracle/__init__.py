@@ -42,10 +42,14 @@ def build(force=False, variant=None):
     lib = os.path.join(OUT_DIR, name)
     hdr = os.path.join(HERE, '..', 'include', 'diffstir.h')
     if (not force and os.path.exists(lib)
-            and os.path.getmtime(lib) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr))):
+            and os.path.getmtime(lib) >= max(os.path.getmtime(SRC), os.path.getmtime(hdr),
+                                             os.path.getmtime(__file__))):
         return lib
     tmp = lib + '.tmp%d' % os.getpid()
-    cmd = ['g++', '-O2', '-std=c++17', '-fopenmp', '-fPIC', '-shared'] + flags + ['-o', tmp, SRC]
+    # -ffp-contract=off: every operation rounded as written (no fused
+    # multiply-adds), so that the FP32 build follows the reference's
+    # per-operation rounding and gives the same results on x86-64 and aarch64
+    cmd = ['g++', '-O2', '-std=c++17', '-ffp-contract=off', '-fopenmp', '-fPIC', '-shared'] + flags + ['-o', tmp, SRC]
     subprocess.run(cmd, check=True)
     os.replace(tmp, lib)
     return lib

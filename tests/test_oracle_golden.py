@@ -20,8 +20,10 @@ FIXTURES = [('ref_f64_g32', 'f64', (0, 1, 2)), ('ref_f32_g32', 'f32', (0, 1, 2))
             ('ref_f64_g16_long', 'f64', (0, 1, 2)), ('ref_f32_g16_long', 'f32', (0, 1, 2))]
 CASES = [(n, p, m) for (n, p, ms) in FIXTURES for m in ms]
 
-# relative tolerances: (force, state, param grad, state grad)
-TOL = {'f64': (2e-6, 2e-6, 2e-6, 2e-6), 'f32': (2e-3, 2e-4, 2e-2, 2e-2)}
+# relative tolerances: (force, state, param grad, state grad).  Measured
+# worst cases over all fixtures and models: f64 1.2e-7 (state), f32 2.0e-6
+# (force and state) and 1.3e-6 (gradients); the bars leave a factor of ten.
+TOL = {'f64': (2e-6, 2e-6, 2e-6, 2e-6), 'f32': (2e-5, 2e-5, 2e-5, 2e-5)}
 
 
 def _rel(a, b):
